@@ -1,0 +1,13 @@
+"""help_gb300: GB300-native normal-equations backend for the HELP interior-point LP solver.
+
+Public entry points:
+
+* :class:`help_gb300.backend.GpuNormalEquations` -- the four boundary
+  operations of the reference's PCG backend (LinearEquation_Construct,
+  RenewLinearEquation, SolveLinearEquation, LinearEquation_Destruct) on one
+  GB300, over the C ABI of ``libhelp_gpu.so`` (include/help_gpu.h);
+* :func:`help_gb300.lp.make_lp` -- the seeded benchmark instances;
+* :func:`help_gb300.hsd.solve_lp` -- the HSD interior-point driver over any
+  backend.
+"""
+__all__ = ["backend", "lp", "hsd", "native", "build"]

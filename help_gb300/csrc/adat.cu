@@ -1,0 +1,151 @@
+// Explicit upper triangle of A diag(w) A^T -- ADAt_Allocate + ADAt_Calc
+// (Helper.cpp:215-377), the assembly the reference's direct backends time.
+//
+// Row i of the triangle collects, for every entry (i, j) of A and every entry
+// (k, j) of column j with k >= i, the product A_ij w_j A_kj.  The reference
+// accumulates these into a dense per-thread array in exactly that order
+// (row entries by increasing j, each column downward).  Here one warp owns
+// one row: it gathers the row's contributions into shared memory tagged with
+// (k, generation index), bitonic-sorts them and sums each run of equal k in
+// generation order, with the multiply and add rounded separately as the
+// reference's loops do; columns come out sorted inside each row.
+//
+// Rows with more than kAdatCap contributions are rejected (the caller gets
+// an error): the normal-equations path never needs the explicit matrix.
+#include "common.cuh"
+#include "kernels.h"
+
+namespace help {
+
+namespace {
+
+constexpr int kAdatCap = 2048;
+constexpr int kAdatWarps = 4;
+
+__device__ __forceinline__ int next_pow2(int v) {
+    int p = 1;
+    while (p < v) p <<= 1;
+    return p;
+}
+
+// Gather (key, value) contributions of row i; returns the count (may exceed cap).
+template <bool VALUES>
+__device__ int adat_gather(int i, const int* __restrict__ rp, const int* __restrict__ ci, const double* __restrict__ av,
+                           const int* __restrict__ cp, const int* __restrict__ ri, const double* __restrict__ avT,
+                           const double* __restrict__ wv, unsigned long long* keys, double* vals) {
+    const int lane = threadIdx.x & 31;
+    int count = 0;
+    for (int e = rp[i]; e < rp[i + 1]; ++e) {
+        const int j = ci[e];
+        const int qb = cp[j], qe = cp[j + 1];
+        // first position in column j with row >= i (rows sorted): binary search
+        int lo = qb, hi = qe;
+        while (lo < hi) {
+            const int mid = (lo + hi) >> 1;
+            if (ri[mid] < i) lo = mid + 1;
+            else hi = mid;
+        }
+        double vd = 0.0;
+        if (VALUES) vd = __dmul_rn(av[e], wv[j]);
+        for (int q = lo + lane; q < qe; q += 32) {
+            const int o = count + (q - lo);
+            if (o < kAdatCap) {
+                keys[o] = ((unsigned long long)(unsigned)ri[q] << 32) | (unsigned)o;
+                if (VALUES) vals[o] = __dmul_rn(vd, avT[q]);
+            }
+        }
+        count += qe - lo;
+    }
+    __syncwarp();
+    return count;
+}
+
+__device__ void warp_bitonic(unsigned long long* keys, double* vals, int n, bool with_vals) {
+    const int lane = threadIdx.x & 31;
+    for (int size = 2; size <= n; size <<= 1) {
+        for (int stride = size >> 1; stride > 0; stride >>= 1) {
+            for (int t = lane; t < n / 2; t += 32) {
+                const int a = 2 * t - (t & (stride - 1));
+                const int b = a + stride;
+                const bool up = ((a & size) == 0);
+                const unsigned long long ka = keys[a], kb = keys[b];
+                if ((ka > kb) == up) {
+                    keys[a] = kb;
+                    keys[b] = ka;
+                    if (with_vals) {
+                        const double va = vals[a];
+                        vals[a] = vals[b];
+                        vals[b] = va;
+                    }
+                }
+            }
+            __syncwarp();
+        }
+    }
+}
+
+template <bool FILL>
+__global__ void k_adat(const int* __restrict__ rp, const int* __restrict__ ci, const double* __restrict__ av,
+                       const int* __restrict__ cp, const int* __restrict__ ri, const double* __restrict__ avT,
+                       const double* __restrict__ wv, int m, int* __restrict__ cnt, const int* __restrict__ out_rp,
+                       int* __restrict__ out_ci, double* __restrict__ out_v) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const size_t per = (size_t)kAdatCap * (8 + (FILL ? 8 : 0));
+    unsigned long long* keys = reinterpret_cast<unsigned long long*>(smem + per * warp);
+    double* vals = reinterpret_cast<double*>(keys + kAdatCap);
+    for (int64_t i = (int64_t)blockIdx.x * nw + warp; i < m; i += (int64_t)gridDim.x * nw) {
+        const int n = adat_gather<FILL>((int)i, rp, ci, av, cp, ri, avT, wv, keys, vals);
+        if (n > kAdatCap) {
+            if (!FILL && lane == 0) cnt[i] = -1;
+            continue;
+        }
+        const int np = next_pow2(n);
+        for (int t = n + lane; t < np; t += 32) keys[t] = ~0ull;
+        __syncwarp();
+        warp_bitonic(keys, vals, np, FILL);
+        // runs of equal column: lane-parallel head flags, sequential sums per run
+        int pos = FILL ? out_rp[i] : 0;
+        for (int base = 0; base < n; base += 32) {
+            const int t = base + lane;
+            const bool head = (t < n) && (t == 0 || (keys[t] >> 32) != (keys[t - 1] >> 32));
+            const unsigned ball = __ballot_sync(0xffffffffu, head);
+            if (FILL && head) {
+                const unsigned kcol = (unsigned)(keys[t] >> 32);
+                double s = 0.0;
+                for (int u = t; u < n && (unsigned)(keys[u] >> 32) == kcol; ++u) s = __dadd_rn(s, vals[u]);
+                const int o = pos + __popc(ball & ((1u << lane) - 1u));
+                out_ci[o] = (int)kcol;
+                out_v[o] = s;
+            }
+            pos += __popc(ball);
+        }
+        if (!FILL && lane == 0) cnt[i] = pos;
+        __syncwarp();
+    }
+}
+
+}  // namespace
+
+cudaError_t adat_count(const int* rp, const int* ci, const int* cp, const int* ri, int m, int* cnt, cudaStream_t st) {
+    const size_t smem = (size_t)kAdatCap * 8 * kAdatWarps;
+    cudaError_t e = cudaFuncSetAttribute(k_adat<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    const int blocks = (m + kAdatWarps - 1) / kAdatWarps < 4096 ? (m + kAdatWarps - 1) / kAdatWarps : 4096;
+    k_adat<false><<<blocks > 0 ? blocks : 1, 32 * kAdatWarps, smem, st>>>(rp, ci, nullptr, cp, ri, nullptr, nullptr, m,
+                                                                         cnt, nullptr, nullptr, nullptr);
+    return cudaGetLastError();
+}
+
+cudaError_t adat_fill(const int* rp, const int* ci, const double* av, const int* cp, const int* ri, const double* avT,
+                      const double* wv, int m, const int* out_rp, int* out_ci, double* out_v, cudaStream_t st) {
+    const size_t smem = (size_t)kAdatCap * 16 * kAdatWarps;
+    cudaError_t e = cudaFuncSetAttribute(k_adat<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    const int blocks = (m + kAdatWarps - 1) / kAdatWarps < 4096 ? (m + kAdatWarps - 1) / kAdatWarps : 4096;
+    k_adat<true><<<blocks > 0 ? blocks : 1, 32 * kAdatWarps, smem, st>>>(rp, ci, av, cp, ri, avT, wv, m, nullptr,
+                                                                        out_rp, out_ci, out_v);
+    return cudaGetLastError();
+}
+
+}  // namespace help

@@ -1,0 +1,831 @@
+// C ABI of libhelp_gpu.so (declared in include/help_gpu.h).
+//
+// Boundary: the reference's PCG backend (UsePCG_CPU.cpp:26-183 + PCG.cpp).
+// Host arrays in, host arrays out; everything else stays on the GPU.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "context.h"
+#include "items.h"
+#include "kernels.h"
+#include "spmv.cuh"
+
+using namespace help;
+
+namespace {
+
+constexpr int kPartElems = 8192;  // per-block partial sums and reduction scratch
+
+int fail(help_pcg* ctx, int code, const std::string& msg) {
+    if (ctx) ctx->err = msg;
+    return code;
+}
+int fail_cuda(help_pcg* ctx, cudaError_t e, const char* what) {
+    if (ctx) ctx->err = std::string(what) + ": " + cudaGetErrorString(e);
+    return e == cudaErrorMemoryAllocation ? HELP_E_NOMEM : HELP_E_CUDA;
+}
+
+#define CK(call)                                                  \
+    do {                                                          \
+        cudaError_t _e = (call);                                  \
+        if (_e != cudaSuccess) return fail_cuda(ctx, _e, #call); \
+    } while (0)
+
+double now_ms() {
+    return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+DevCtrl* ctrl_of(help_pcg* ctx) { return ctx->ctrl.as<DevCtrl>(); }
+
+int upload_items(help_pcg* ctx, ItemList& L, const int32_t* ptr, int32_t rows, int cap) {
+    std::vector<Int4> v = plan_items(ptr, rows, cap, 512, 48);
+    L.n = (int32_t)v.size();
+    L.cap = cap;
+    CK(L.buf.ensure(sizeof(Int4) * std::max<size_t>(v.size(), 1)));
+    if (!v.empty()) CK(cudaMemcpyAsync(L.buf.p, v.data(), sizeof(Int4) * v.size(), cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));  // v goes out of scope
+    return HELP_OK;
+}
+
+int ensure_stage(help_pcg* ctx, size_t elems) {
+    if (ctx->h_stage_elems >= elems) return HELP_OK;
+    if (ctx->h_stage) cudaFreeHost(ctx->h_stage);
+    ctx->h_stage = nullptr;
+    ctx->h_stage_elems = 0;
+    CK(cudaMallocHost((void**)&ctx->h_stage, sizeof(double) * elems));
+    ctx->h_stage_elems = elems;
+    return HELP_OK;
+}
+
+// host -> device through the pinned staging buffer
+int h2d(help_pcg* ctx, double* dst, const double* src, size_t n) {
+    int rc = ensure_stage(ctx, n);
+    if (rc) return rc;
+    std::memcpy(ctx->h_stage, src, sizeof(double) * n);
+    CK(cudaMemcpyAsync(dst, ctx->h_stage, sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return HELP_OK;
+}
+int d2h(help_pcg* ctx, double* dst, const double* src, size_t n) {
+    int rc = ensure_stage(ctx, n);
+    if (rc) return rc;
+    CK(cudaMemcpyAsync(ctx->h_stage, src, sizeof(double) * n, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    std::memcpy(dst, ctx->h_stage, sizeof(double) * n);
+    return HELP_OK;
+}
+
+int read_status(help_pcg* ctx, const char* where) {
+    int st = 0;
+    CK(cudaMemcpyAsync(&st, &ctrl_of(ctx)->status, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    if (st != 0) {
+        CK(cudaMemsetAsync(&ctrl_of(ctx)->status, 0, sizeof(int), ctx->stream));
+        CK(cudaStreamSynchronize(ctx->stream));
+        return fail(ctx, st == kStatusTimeout ? HELP_E_TIMEOUT : HELP_E_NUMERIC,
+                    std::string(where) + (st == kStatusTimeout ? ": device wait timed out" : ": numerical failure"));
+    }
+    return HELP_OK;
+}
+
+// ---------------------------------------------------------------- CG runs
+
+struct CgResult {
+    long long iterations = 0;
+    double rr0 = 0, rr = 0;
+    int converged = 0;
+    int status = 0;
+};
+
+template <class V>
+int run_pcg(help_pcg* ctx, V* x, V* r0, double tol, long long max_iter, int precond_only, CgResult* res) {
+    const bool f32 = std::is_same<V, float>::value;
+    PcgArgs<V> A{};
+    A.m = ctx->m;
+    A.n = ctx->n;
+    A.k = ctx->k;
+    const ItemList& icsr = f32 ? ctx->it_csr32 : ctx->it_csr;
+    const ItemList& icsc = f32 ? ctx->it_csc32 : ctx->it_csc;
+    const ItemList& ic = f32 ? ctx->it_c32 : ctx->it_c;
+    const ItemList& ict = f32 ? ctx->it_ct32 : ctx->it_ct;
+    A.cap = icsr.cap;
+    A.csr_items = icsr.items();
+    A.n_csr = icsr.n;
+    A.rp = ctx->rp.as<int>();
+    A.ci = ctx->ci.as<int>();
+    A.bv = f32 ? (const V*)ctx->bv32.p : (const V*)ctx->bv.p;
+    A.csc_items = icsc.items();
+    A.n_csc = icsc.n;
+    A.cp = ctx->cp.as<int>();
+    A.ri = ctx->ri.as<int>();
+    A.bvT = f32 ? (const V*)ctx->bvT32.p : (const V*)ctx->bvT.p;
+    A.c_items = ic.items();
+    A.n_c = ic.n;
+    A.c_rp = ctx->c_rp.as<int>();
+    A.c_ci = ctx->c_ci.as<int>();
+    A.c_v = f32 ? (const V*)ctx->c_v32.p : (const V*)ctx->c_v.p;
+    A.ct_items = ict.items();
+    A.n_ct = ict.n;
+    A.ct_rp = ctx->ct_rp.as<int>();
+    A.ct_ci = ctx->ct_ci.as<int>();
+    A.ct_v = f32 ? (const V*)ctx->ct_v32.p : (const V*)ctx->ct_v.p;
+    A.piv = ctx->piv.as<int>();
+    A.pivpos = ctx->pivpos.as<int>();
+    A.W = ctx->W.as<double>();
+    A.dsinv = f32 ? (const V*)ctx->dsinv32.p : (const V*)ctx->dsinv.p;
+    A.delta = ctx->opt.delta;
+    A.tol2 = tol * tol;
+    A.max_iter = max_iter;
+    A.x = x;
+    A.r0 = r0;
+    A.r1 = f32 ? (V*)ctx->r132.p : (V*)ctx->r1.p;
+    A.z = f32 ? (V*)ctx->z32.p : (V*)ctx->z.p;
+    A.p0 = f32 ? (V*)ctx->p032.p : (V*)ctx->p0.p;
+    A.p1 = f32 ? (V*)ctx->p132.p : (V*)ctx->p1.p;
+    A.q = f32 ? (V*)ctx->q32.p : (V*)ctx->q.p;
+    A.t = f32 ? (V*)ctx->t32.p : (V*)ctx->t.p;
+    A.a = ctx->a.as<double>();
+    A.w = ctx->w.as<double>();
+    A.part = ctx->partials.as<double>();
+    A.precond_only = precond_only;
+    DevCtrl* c = ctrl_of(ctx);
+    A.bar.count = &c->bar_count;
+    A.bar.gen = &c->bar_gen;
+    A.bar.status = &c->status;
+    A.out = &c->cg;
+    const int blocks = f32 ? ctx->coop_blocks_f32 : ctx->coop_blocks_f64;
+    const size_t smem = std::max(spmv_smem_bytes<V>(A.cap), (size_t)std::max(ctx->k, 1) * sizeof(double));
+    if ((size_t)blocks * 3 > (size_t)kPartElems) return fail(ctx, HELP_E_ARG, "too many persistent blocks");
+    CK(cudaMemsetAsync(c, 0, 2 * sizeof(unsigned int), ctx->stream));
+    CK(pcg_launch<V>(A, blocks, ctx->threads, smem, ctx->stream));
+    CgOutDev out{};
+    CK(cudaMemcpyAsync(&out, &c->cg, sizeof(out), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    int rc = read_status(ctx, "pcg");
+    if (rc) return rc;
+    res->iterations = out.iterations;
+    res->rr0 = out.rr0;
+    res->rr = out.rr;
+    res->converged = out.converged;
+    res->status = out.status;
+    if (out.status != 0) return fail(ctx, HELP_E_NUMERIC, "pcg: breakdown (non-positive curvature or NaN)");
+    return HELP_OK;
+}
+
+// res = rhs - G x  (FP64), returns ||res||^2 in *rr (host)
+int residual_f64(help_pcg* ctx, const double* x, const double* rhs, double* res, double* rr) {
+    CK(spmv_launch<double>(kEpiStore, ctx->it_csc.items(), ctx->it_csc.n, ctx->cp.as<int>(), ctx->ri.as<int>(),
+                           ctx->bvT.as<double>(), ctx->it_csc.cap, x, ctx->t.as<double>(), nullptr, nullptr, nullptr,
+                           0.0, 0, ctx->threads, ctx->stream));
+    CK(spmv_launch<double>(kEpiResid, ctx->it_csr.items(), ctx->it_csr.n, ctx->rp.as<int>(), ctx->ci.as<int>(),
+                           ctx->bv.as<double>(), ctx->it_csr.cap, ctx->t.as<double>(), res, rhs, x, nullptr,
+                           ctx->opt.delta, 0, ctx->threads, ctx->stream));
+    if (rr) {
+        double* part = ctx->partials.as<double>() + 4096;
+        CK(vec_sumsq(res, ctx->m, part, part + 2048, ctx->stream));
+        CK(cudaMemcpyAsync(rr, part + 2048, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+        CK(cudaStreamSynchronize(ctx->stream));
+    }
+    return HELP_OK;
+}
+
+int sumsq_host(help_pcg* ctx, const double* v, int64_t n, double* out) {
+    double* part = ctx->partials.as<double>() + 4096;
+    CK(vec_sumsq(v, n, part, part + 2048, ctx->stream));
+    CK(cudaMemcpyAsync(out, part + 2048, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return HELP_OK;
+}
+
+// Solve G x = rhs on the device; x holds the start (zero unless warm).
+int normal_solve(help_pcg* ctx, const double* rhs, double* x, bool warm, long long* iters_out, int* outer_out,
+                 int* fell_back, int* converged_out) {
+    const int m = ctx->m;
+    long long iters = 0;
+    int rc;
+    *fell_back = 0;
+    *outer_out = 0;
+    double* r = ctx->r0.as<double>();
+    double rhs2 = 0.0;
+    rc = sumsq_host(ctx, rhs, m, &rhs2);
+    if (rc) return rc;
+    if (ctx->opt.precision == HELP_PREC_FP64) {
+        CgResult res;
+        double tol = ctx->opt.cg_tol;
+        if (warm) {
+            double rr = 0.0;
+            rc = residual_f64(ctx, x, rhs, r, &rr);
+            if (rc) return rc;
+            // keep the reference's target ||r|| < tol * ||rhs|| relative to the cold start
+            tol = (rr > 0.0) ? ctx->opt.cg_tol * std::sqrt(rhs2 / rr) : 1.0;
+        } else {
+            CK(cudaMemcpyAsync(r, rhs, sizeof(double) * m, cudaMemcpyDeviceToDevice, ctx->stream));
+            CK(vec_fill(x, 0.0, m, ctx->stream));
+        }
+        rc = run_pcg<double>(ctx, x, r, tol, ctx->opt.cg_max_iter, 0, &res);
+        if (rc) return rc;
+        *iters_out = res.iterations;
+        *converged_out = res.converged;
+        return HELP_OK;
+    }
+    // Mixed precision: FP32 CG corrections inside FP64 iterative refinement.
+    if (!warm) CK(vec_fill(x, 0.0, m, ctx->stream));
+    double rr = 0.0;
+    rc = residual_f64(ctx, x, rhs, r, &rr);
+    if (rc) return rc;
+    const double target2 = ctx->opt.ir_tol * ctx->opt.ir_tol * rhs2;
+    int outer = 0;
+    bool ok = (rr <= target2) || rhs2 == 0.0;
+    double prev = rr;
+    while (!ok && outer < ctx->opt.ir_max_outer) {
+        // scale the residual to unit norm before narrowing to FP32
+        const double scale = std::sqrt(rr);
+        CK(vec_to_f32_scaled(r, 1.0 / scale, ctx->r032.as<float>(), m, ctx->stream));
+        CgResult res;
+        CK(vec_fill_f32(ctx->x32.as<float>(), 0.0f, m, ctx->stream));
+        rc = run_pcg<float>(ctx, ctx->x32.as<float>(), ctx->r032.as<float>(), ctx->opt.inner_tol,
+                            ctx->opt.inner_max_iter, 0, &res);
+        if (rc) return rc;
+        iters += res.iterations;
+        CK(vec_add_f32_scaled(x, ctx->x32.as<float>(), scale, m, ctx->stream));
+        rc = residual_f64(ctx, x, rhs, r, &rr);
+        if (rc) return rc;
+        ++outer;
+        ok = (rr <= target2);
+        if (!ok && !(rr < 0.25 * prev)) break;  // stagnation: FP32 corrections no longer help
+        prev = rr;
+    }
+    *outer_out = outer;
+    if (!ok && ctx->opt.fallback) {
+        CgResult res;
+        const double tol = (rr > 0.0) ? ctx->opt.ir_tol * std::sqrt(rhs2 / rr) : 1.0;
+        rc = run_pcg<double>(ctx, x, r, std::min(tol, 1.0), ctx->opt.cg_max_iter, 0, &res);
+        if (rc) return rc;
+        iters += res.iterations;
+        *fell_back = 1;
+        ok = res.converged != 0;
+    }
+    *iters_out = iters;
+    *converged_out = ok ? 1 : 0;
+    return HELP_OK;
+}
+
+int alloc_vectors(help_pcg* ctx) {
+    const size_t m = ctx->m, n = ctx->n;
+    const size_t mn = std::max(m, n);
+    CK(ctx->x.ensure(8 * m));
+    CK(ctx->r0.ensure(8 * m));
+    CK(ctx->r1.ensure(8 * m));
+    CK(ctx->z.ensure(8 * m));
+    CK(ctx->p0.ensure(8 * m));
+    CK(ctx->p1.ensure(8 * m));
+    CK(ctx->q.ensure(8 * m));
+    CK(ctx->t.ensure(8 * n));
+    CK(ctx->u.ensure(8 * n));
+    CK(ctx->rhs.ensure(8 * m));
+    CK(ctx->b1.ensure(8 * n));
+    CK(ctx->b2.ensure(8 * m));
+    CK(ctx->x1.ensure(8 * n));
+    CK(ctx->x2.ensure(8 * mn));
+    CK(ctx->res.ensure(8 * mn));
+    CK(ctx->xacc.ensure(8 * mn));
+    CK(ctx->d.ensure(8 * n));
+    CK(ctx->s.ensure(8 * n));
+    CK(ctx->diag.ensure(8 * m));
+    CK(ctx->dsinv.ensure(8 * m));
+    CK(ctx->piv.ensure(4 * m));
+    CK(ctx->pivpos.ensure(4 * m));
+    CK(ctx->keys.ensure(8 * m));
+    CK(ctx->hist.ensure(4 * kTopkBins));
+    CK(ctx->flags.ensure(4 * 3 * mn + 64));
+    CK(ctx->scan_tmp.ensure(4 * scan_tmp_elems((int64_t)std::max<size_t>(mn + 1, 1u << 20) * 4)));
+    CK(ctx->cr_cnt.ensure(4 * (mn + 1)));
+    CK(ctx->bp_ptr.ensure(4 * (n + 1)));
+    CK(ctx->c_rp.ensure(4 * (m + 1)));
+    if (ctx->opt.precision == HELP_PREC_MIXED) {
+        CK(ctx->x32.ensure(4 * m));
+        CK(ctx->r032.ensure(4 * m));
+        CK(ctx->r132.ensure(4 * m));
+        CK(ctx->z32.ensure(4 * m));
+        CK(ctx->p032.ensure(4 * m));
+        CK(ctx->p132.ensure(4 * m));
+        CK(ctx->q32.ensure(4 * m));
+        CK(ctx->t32.ensure(4 * n));
+        CK(ctx->dsinv32.ensure(4 * m));
+    }
+    return HELP_OK;
+}
+
+void release_all(help_pcg* ctx) {
+    DevMem* bufs[] = {&ctx->rp,     &ctx->ci,    &ctx->av,     &ctx->cp,     &ctx->ri,    &ctx->avT,   &ctx->bv,
+                      &ctx->bvT,    &ctx->bv32,  &ctx->bvT32,  &ctx->d,      &ctx->s,     &ctx->diag,  &ctx->dsinv,
+                      &ctx->dsinv32, &ctx->piv,  &ctx->pivpos, &ctx->keys,   &ctx->hist,  &ctx->flags, &ctx->scan_tmp,
+                      &ctx->bp_ptr, &ctx->bp_c,  &ctx->bp_v,   &ctx->cr_cnt, &ctx->c_rp,  &ctx->c_ci,  &ctx->c_v,
+                      &ctx->c_v32,  &ctx->ct_rp, &ctx->ct_ci,  &ctx->ct_v,   &ctx->ct_v32, &ctx->ct_blk, &ctx->g11,
+                      &ctx->W,      &ctx->lwork, &ctx->x,      &ctx->r0,     &ctx->r1,    &ctx->z,     &ctx->p0,
+                      &ctx->p1,     &ctx->q,     &ctx->t,      &ctx->a,      &ctx->w,     &ctx->x32,   &ctx->r032,
+                      &ctx->r132,   &ctx->z32,   &ctx->p032,   &ctx->p132,   &ctx->q32,   &ctx->t32,   &ctx->u,
+                      &ctx->rhs,    &ctx->b1,    &ctx->b2,     &ctx->x1,     &ctx->x2,    &ctx->res,   &ctx->xacc,
+                      &ctx->adat_tmp};
+    for (DevMem* b : bufs) b->release();
+    ItemList* lists[] = {&ctx->it_csr, &ctx->it_csc, &ctx->it_csr32, &ctx->it_csc32,
+                         &ctx->it_c,   &ctx->it_ct,  &ctx->it_c32,   &ctx->it_ct32};
+    for (ItemList* l : lists) {
+        l->buf.release();
+        l->n = 0;
+    }
+}
+
+int read_int(help_pcg* ctx, const int* dev, int* out) {
+    CK(cudaMemcpyAsync(out, dev, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return HELP_OK;
+}
+
+int renew_impl(help_pcg* ctx, const double* d_host) {
+    const double t0 = now_ms();
+    const int m = ctx->m, n = ctx->n;
+    const bool mixed = ctx->opt.precision == HELP_PREC_MIXED;
+    DevCtrl* c = ctrl_of(ctx);
+    int rc = h2d(ctx, ctx->d.as<double>(), d_host, n);
+    if (rc) return rc;
+    CK(renew_inv_sqrt(ctx->d.as<double>(), ctx->s.as<double>(), n, &c->status, ctx->stream));
+    rc = read_status(ctx, "renew: d must be positive and finite");
+    if (rc) return rc;
+    CK(renew_scale_values(ctx->s.as<double>(), ctx->rp.as<int>(), ctx->ci.as<int>(), ctx->av.as<double>(),
+                          ctx->bv.as<double>(), mixed ? ctx->bv32.as<float>() : nullptr, ctx->cp.as<int>(),
+                          ctx->avT.as<double>(), ctx->bvT.as<double>(), mixed ? ctx->bvT32.as<float>() : nullptr,
+                          ctx->diag.as<double>(), ctx->opt.delta, m, n, ctx->nnz, ctx->stream));
+    // pivots
+    const int k = std::max(0, std::min(ctx->opt.pivots, m));
+    ctx->k = k;
+    CK(topk_select(ctx->diag.as<double>(), m, k, ctx->keys.as<unsigned long long>(), ctx->hist.as<unsigned int>(),
+                   ctx->flags.as<int>(), ctx->scan_tmp.as<int>(), &c->topk, &c->status, ctx->piv.as<int>(),
+                   ctx->pivpos.as<int>(), ctx->stream));
+    rc = read_status(ctx, "renew: diag(A D^-1 A^T) not finite");
+    if (rc) return rc;
+    // pivot entries per column
+    int* cnt = ctx->cr_cnt.as<int>();
+    CK(pivot_lists_count(ctx->cp.as<int>(), ctx->ri.as<int>(), ctx->pivpos.as<int>(), n, cnt, ctx->stream));
+    CK(exclusive_scan(cnt, ctx->bp_ptr.as<int>(), n, ctx->scan_tmp.as<int>(), &c->totals[0], ctx->stream));
+    int nbp = 0;
+    rc = read_int(ctx, &c->totals[0], &nbp);
+    if (rc) return rc;
+    CK(cudaMemcpyAsync(ctx->bp_ptr.as<int>() + n, &c->totals[0], sizeof(int), cudaMemcpyDeviceToDevice, ctx->stream));
+    CK(ctx->bp_c.ensure(4 * (size_t)std::max(nbp, 1)));
+    CK(ctx->bp_v.ensure(8 * (size_t)std::max(nbp, 1)));
+    CK(pivot_lists_fill(ctx->cp.as<int>(), ctx->ri.as<int>(), ctx->bvT.as<double>(), ctx->pivpos.as<int>(), n,
+                        ctx->bp_ptr.as<int>(), ctx->bp_c.as<int>(), ctx->bp_v.as<double>(), ctx->stream));
+    // G[i, P]: counts, row pointers of C, fill (C rows and dense G11)
+    CK(ctx->g11.ensure(8 * (size_t)std::max(k, 1) * std::max(k, 1)));
+    CK(ctx->W.ensure(8 * (size_t)std::max(k, 1) * std::max(k, 1)));
+    CK(ctx->lwork.ensure(8 * dense_work_elems(std::max(k, 1))));
+    CK(ctx->a.ensure(8 * (size_t)std::max(k, 1)));
+    CK(ctx->w.ensure(8 * (size_t)std::max(k, 1)));
+    CK(gcols_rows(0, ctx->rp.as<int>(), ctx->ci.as<int>(), ctx->bv.as<double>(), ctx->bp_ptr.as<int>(),
+                  ctx->bp_c.as<int>(), ctx->bp_v.as<double>(), ctx->pivpos.as<int>(), m, k, ctx->opt.delta, cnt,
+                  nullptr, nullptr, nullptr, nullptr, ctx->num_sms, ctx->stream));
+    CK(exclusive_scan(cnt, ctx->c_rp.as<int>(), m, ctx->scan_tmp.as<int>(), &c->totals[1], ctx->stream));
+    int nnzc = 0;
+    rc = read_int(ctx, &c->totals[1], &nnzc);
+    if (rc) return rc;
+    CK(cudaMemcpyAsync(ctx->c_rp.as<int>() + m, &c->totals[1], sizeof(int), cudaMemcpyDeviceToDevice, ctx->stream));
+    ctx->nnz_c = nnzc;
+    CK(ctx->c_ci.ensure(4 * (size_t)std::max(nnzc, 1)));
+    CK(ctx->c_v.ensure(8 * (size_t)std::max(nnzc, 1)));
+    if (k > 0) CK(cudaMemsetAsync(ctx->g11.p, 0, 8 * (size_t)k * k, ctx->stream));
+    CK(gcols_rows(1, ctx->rp.as<int>(), ctx->ci.as<int>(), ctx->bv.as<double>(), ctx->bp_ptr.as<int>(),
+                  ctx->bp_c.as<int>(), ctx->bp_v.as<double>(), ctx->pivpos.as<int>(), m, k, ctx->opt.delta, nullptr,
+                  ctx->c_rp.as<int>(), ctx->c_ci.as<int>(), ctx->c_v.as<double>(), ctx->g11.as<double>(),
+                  ctx->num_sms, ctx->stream));
+    // C^T
+    CK(ctx->ct_rp.ensure(4 * (size_t)(k + 1)));
+    CK(ctx->ct_ci.ensure(4 * (size_t)std::max(nnzc, 1)));
+    CK(ctx->ct_v.ensure(8 * (size_t)std::max(nnzc, 1)));
+    if (k > 0) {
+        const int nblk = (m + ct_rows_per_block() - 1) / ct_rows_per_block();
+        const size_t nb = (size_t)k * nblk;
+        CK(ctx->ct_blk.ensure(4 * (2 * nb + 2)));
+        CK(ctx->scan_tmp.ensure(4 * std::max(scan_tmp_elems((int64_t)nb), scan_tmp_elems((int64_t)std::max(m, n) + 1))));
+        int* blk_cnt = ctx->ct_blk.as<int>();
+        int* blk_off = blk_cnt + nb + 1;
+        CK(ct_count(ctx->c_rp.as<int>(), ctx->c_ci.as<int>(), m, k, blk_cnt, ctx->stream));
+        CK(exclusive_scan(blk_cnt, blk_off, (int64_t)nb, ctx->scan_tmp.as<int>(), &c->totals[2], ctx->stream));
+        CK(ct_row_ptr(blk_off, k, nblk, &c->totals[2], ctx->ct_rp.as<int>(), ctx->stream));
+        CK(ct_fill(ctx->c_rp.as<int>(), ctx->c_ci.as<int>(), ctx->c_v.as<double>(), m, k, blk_off,
+                   ctx->ct_ci.as<int>(), ctx->ct_v.as<double>(), ctx->stream));
+    } else {
+        CK(cudaMemsetAsync(ctx->ct_rp.p, 0, 4, ctx->stream));
+    }
+    if (mixed) {
+        CK(ctx->c_v32.ensure(4 * (size_t)std::max(nnzc, 1)));
+        CK(ctx->ct_v32.ensure(4 * (size_t)std::max(nnzc, 1)));
+        CK(vals_to_f32(ctx->c_v.as<double>(), ctx->c_v32.as<float>(), nnzc, ctx->stream));
+        CK(vals_to_f32(ctx->ct_v.as<double>(), ctx->ct_v32.as<float>(), nnzc, ctx->stream));
+    }
+    // plans for C and C^T
+    ctx->h_tmp.resize((size_t)m + 1);
+    CK(cudaMemcpyAsync(ctx->h_tmp.data(), ctx->c_rp.p, 4 * ((size_t)m + 1), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    rc = upload_items(ctx, ctx->it_c, ctx->h_tmp.data(), m, kCapF64);
+    if (rc) return rc;
+    if (mixed) {
+        rc = upload_items(ctx, ctx->it_c32, ctx->h_tmp.data(), m, kCapF32);
+        if (rc) return rc;
+    }
+    std::vector<int32_t> ctp((size_t)k + 1, 0);
+    if (k > 0) {
+        CK(cudaMemcpyAsync(ctp.data(), ctx->ct_rp.p, 4 * ((size_t)k + 1), cudaMemcpyDeviceToHost, ctx->stream));
+        CK(cudaStreamSynchronize(ctx->stream));
+    }
+    rc = upload_items(ctx, ctx->it_ct, ctp.data(), k, kCapF64);
+    if (rc) return rc;
+    if (mixed) {
+        rc = upload_items(ctx, ctx->it_ct32, ctp.data(), k, kCapF32);
+        if (rc) return rc;
+    }
+    // pivot block inverse and the Schur diagonal
+    CK(cudaMemsetAsync(&c->regularised, 0, sizeof(int), ctx->stream));
+    if (k > 0)
+        CK(dense_spd_inverse(ctx->g11.as<double>(), ctx->W.as<double>(), ctx->lwork.as<double>(), k, &c->regularised,
+                             ctx->stream));
+    CK(schur_diag(ctx->c_rp.as<int>(), ctx->c_ci.as<int>(), ctx->c_v.as<double>(), ctx->W.as<double>(),
+                  ctx->diag.as<double>(), ctx->pivpos.as<int>(), m, k, 1.0e-14, ctx->dsinv.as<double>(),
+                  mixed ? ctx->dsinv32.as<float>() : nullptr, ctx->stream));
+    rc = read_int(ctx, &c->regularised, &ctx->dense_regularised);
+    if (rc) return rc;
+    CK(cudaGetLastError());
+    ctx->renewed = true;
+    ctx->have_prev_x2 = false;
+    ctx->stats.renews++;
+    ctx->stats.renew_ms = now_ms() - t0;
+    ctx->stats.nnz_c = ctx->nnz_c;
+    ctx->stats.pivots = k;
+    return HELP_OK;
+}
+
+}  // namespace
+
+// ================================================================ C ABI
+
+extern "C" {
+
+void help_pcg_default_options(help_pcg_options* o) {
+    if (!o) return;
+    std::memset(o, 0, sizeof(*o));
+    o->device = 0;
+    o->pivots = 10;
+    o->precision = HELP_PREC_FP64;
+    o->cg_tol = 1e-20;
+    o->cg_max_iter = 1000000;
+    o->delta = 0.0;
+    o->ir_tol = 1e-10;
+    o->ir_max_outer = 10;
+    o->inner_tol = 1e-5;
+    o->inner_max_iter = 200000;
+    o->warm_start = 0;
+    o->fallback = 1;
+    o->threads = 0;
+}
+
+int help_pcg_create(const help_pcg_options* opt, help_pcg** out) {
+    if (!out) return HELP_E_ARG;
+    *out = nullptr;
+    help_pcg* ctx = new (std::nothrow) help_pcg();
+    if (!ctx) return HELP_E_NOMEM;
+    if (opt) ctx->opt = *opt;
+    else help_pcg_default_options(&ctx->opt);
+    if (ctx->opt.precision != HELP_PREC_FP64 && ctx->opt.precision != HELP_PREC_MIXED) {
+        delete ctx;
+        return HELP_E_ARG;
+    }
+    ctx->device = ctx->opt.device;
+    cudaError_t e = cudaSetDevice(ctx->device);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, ctx->device);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = ctx->ctrl.ensure(sizeof(DevCtrl));
+    if (e == cudaSuccess) e = cudaMemset(ctx->ctrl.p, 0, sizeof(DevCtrl));
+    if (e == cudaSuccess) e = ctx->partials.ensure(8 * (size_t)kPartElems);
+    if (e != cudaSuccess) {
+        release_all(ctx);
+        if (ctx->stream) cudaStreamDestroy(ctx->stream);
+        delete ctx;
+        return e == cudaErrorMemoryAllocation ? HELP_E_NOMEM : HELP_E_CUDA;
+    }
+    ctx->threads = ctx->opt.threads > 0 ? ctx->opt.threads : 512;
+    *out = ctx;
+    return HELP_OK;
+}
+
+void help_pcg_free(help_pcg* ctx) {
+    if (!ctx) return;
+    cudaSetDevice(ctx->device);
+    help_pcg_destruct(ctx);
+    ctx->ctrl.release();
+    ctx->partials.release();
+    if (ctx->h_stage) cudaFreeHost(ctx->h_stage);
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+}
+
+int help_pcg_construct(help_pcg* ctx, int32_t m, int32_t n, const int32_t* col_ptr, const int32_t* row_ind,
+                       const double* val) {
+    if (!ctx) return HELP_E_ARG;
+    if (ctx->constructed) return fail(ctx, HELP_E_ARG, "construct: already constructed (call destruct first)");
+    if (m <= 0 || n <= 0 || !col_ptr || !row_ind || !val) return fail(ctx, HELP_E_ARG, "construct: bad arguments");
+    if (col_ptr[0] != 0) return fail(ctx, HELP_E_ARG, "construct: col_ptr[0] must be 0");
+    for (int32_t j = 0; j < n; ++j)
+        if (col_ptr[j + 1] < col_ptr[j]) return fail(ctx, HELP_E_ARG, "construct: col_ptr not monotone");
+    const int64_t nnz = col_ptr[n];
+    for (int32_t j = 0; j < n; ++j)
+        for (int32_t p = col_ptr[j]; p < col_ptr[j + 1]; ++p) {
+            if (row_ind[p] < 0 || row_ind[p] >= m) return fail(ctx, HELP_E_ARG, "construct: row index out of range");
+            if (p > col_ptr[j] && row_ind[p] <= row_ind[p - 1])
+                return fail(ctx, HELP_E_ARG, "construct: rows must be strictly increasing inside a column");
+        }
+    CK(cudaSetDevice(ctx->device));
+    ctx->m = m;
+    ctx->n = n;
+    ctx->nnz = nnz;
+    // CSR(A) from CSC(A) (UsePCG_CPU.cpp:53-66 builds it from the row lists)
+    ctx->h_cp.assign(col_ptr, col_ptr + n + 1);
+    ctx->h_rp.assign((size_t)m + 1, 0);
+    std::vector<int32_t> ci((size_t)std::max<int64_t>(nnz, 1));
+    std::vector<double> av((size_t)std::max<int64_t>(nnz, 1));
+    for (int64_t p = 0; p < nnz; ++p) ctx->h_rp[row_ind[p] + 1]++;
+    for (int32_t i = 0; i < m; ++i) ctx->h_rp[i + 1] += ctx->h_rp[i];
+    {
+        std::vector<int32_t> fill(ctx->h_rp.begin(), ctx->h_rp.end() - 1);
+        for (int32_t j = 0; j < n; ++j)
+            for (int32_t p = col_ptr[j]; p < col_ptr[j + 1]; ++p) {
+                const int32_t q = fill[row_ind[p]]++;
+                ci[q] = j;
+                av[q] = val[p];
+            }
+    }
+    CK(ctx->rp.ensure(4 * ((size_t)m + 1)));
+    CK(ctx->ci.ensure(4 * (size_t)nnz));
+    CK(ctx->av.ensure(8 * (size_t)nnz));
+    CK(ctx->cp.ensure(4 * ((size_t)n + 1)));
+    CK(ctx->ri.ensure(4 * (size_t)nnz));
+    CK(ctx->avT.ensure(8 * (size_t)nnz));
+    CK(ctx->bv.ensure(8 * (size_t)nnz));
+    CK(ctx->bvT.ensure(8 * (size_t)nnz));
+    const bool mixed = ctx->opt.precision == HELP_PREC_MIXED;
+    if (mixed) {
+        CK(ctx->bv32.ensure(4 * (size_t)nnz));
+        CK(ctx->bvT32.ensure(4 * (size_t)nnz));
+    }
+    CK(cudaMemcpyAsync(ctx->rp.p, ctx->h_rp.data(), 4 * ((size_t)m + 1), cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(ctx->ci.p, ci.data(), 4 * (size_t)nnz, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(ctx->av.p, av.data(), 8 * (size_t)nnz, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(ctx->cp.p, col_ptr, 4 * ((size_t)n + 1), cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(ctx->ri.p, row_ind, 4 * (size_t)nnz, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(ctx->avT.p, val, 8 * (size_t)nnz, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    int rc = upload_items(ctx, ctx->it_csr, ctx->h_rp.data(), m, kCapF64);
+    if (!rc) rc = upload_items(ctx, ctx->it_csc, ctx->h_cp.data(), n, kCapF64);
+    if (!rc && mixed) rc = upload_items(ctx, ctx->it_csr32, ctx->h_rp.data(), m, kCapF32);
+    if (!rc && mixed) rc = upload_items(ctx, ctx->it_csc32, ctx->h_cp.data(), n, kCapF32);
+    if (!rc) rc = alloc_vectors(ctx);
+    if (rc) return rc;
+    // persistent grid sizes (every block must be co-resident)
+    int per_sm = 0;
+    const size_t smem64 = std::max(spmv_smem_bytes<double>(kCapF64), (size_t)std::max(ctx->opt.pivots, 1) * 8);
+    CK(pcg_configure<double>(ctx->threads, smem64, &per_sm));
+    if (per_sm < 1) return fail(ctx, HELP_E_ARG, "construct: persistent kernel does not fit on an SM");
+    ctx->coop_blocks_f64 = per_sm * ctx->num_sms;
+    if (mixed) {
+        const size_t smem32 = std::max(spmv_smem_bytes<float>(kCapF32), (size_t)std::max(ctx->opt.pivots, 1) * 8);
+        CK(pcg_configure<float>(ctx->threads, smem32, &per_sm));
+        if (per_sm < 1) return fail(ctx, HELP_E_ARG, "construct: persistent kernel does not fit on an SM");
+        ctx->coop_blocks_f32 = per_sm * ctx->num_sms;
+    }
+    ctx->constructed = true;
+    ctx->renewed = false;
+    return HELP_OK;
+}
+
+int help_pcg_destruct(help_pcg* ctx) {
+    if (!ctx) return HELP_E_ARG;
+    cudaSetDevice(ctx->device);
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    release_all(ctx);
+    ctx->constructed = false;
+    ctx->renewed = false;
+    ctx->last_d = nullptr;
+    ctx->m = ctx->n = 0;
+    ctx->nnz = 0;
+    return HELP_OK;
+}
+
+int help_pcg_renew(help_pcg* ctx, const double* d) {
+    if (!ctx || !d) return HELP_E_ARG;
+    if (!ctx->constructed) return fail(ctx, HELP_E_ARG, "renew: construct first");
+    CK(cudaSetDevice(ctx->device));
+    int rc = renew_impl(ctx, d);
+    if (rc) {
+        ctx->renewed = false;
+        return rc;
+    }
+    ctx->last_d = d;
+    return HELP_OK;
+}
+
+int help_pcg_solve(help_pcg* ctx, const double* d, const double* b_1, const double* b_2, double* x_1,
+                   double* x_2) {
+    if (!ctx || !d || !b_1 || !b_2 || !x_1 || !x_2) return HELP_E_ARG;
+    if (!ctx->constructed) return fail(ctx, HELP_E_ARG, "solve: construct first");
+    CK(cudaSetDevice(ctx->device));
+    int rc;
+    if (!ctx->renewed || d != ctx->last_d) {
+        rc = help_pcg_renew(ctx, d);
+        if (rc) return rc;
+    }
+    const double t0 = now_ms();
+    const int m = ctx->m, n = ctx->n;
+    rc = h2d(ctx, ctx->b1.as<double>(), b_1, n);
+    if (!rc) rc = h2d(ctx, ctx->b2.as<double>(), b_2, m);
+    if (rc) return rc;
+    // u = D^-1/2 b_1 ;  rhs = B u - b_2 = A D^-1 b_1 - b_2   (UsePCG_CPU.cpp:103-112)
+    CK(vec_scale_mul(ctx->s.as<double>(), ctx->b1.as<double>(), ctx->u.as<double>(), n, ctx->stream));
+    CK(spmv_launch<double>(kEpiRhs, ctx->it_csr.items(), ctx->it_csr.n, ctx->rp.as<int>(), ctx->ci.as<int>(),
+                           ctx->bv.as<double>(), ctx->it_csr.cap, ctx->u.as<double>(), ctx->rhs.as<double>(),
+                           ctx->b2.as<double>(), nullptr, nullptr, 0.0, 0, ctx->threads, ctx->stream));
+    // x_2 (UsePCG_CPU.cpp:154-166)
+    const bool warm = ctx->opt.warm_start && ctx->have_prev_x2;
+    long long iters = 0;
+    int outer = 0, fell_back = 0, converged = 0;
+    rc = normal_solve(ctx, ctx->rhs.as<double>(), ctx->x.as<double>(), warm, &iters, &outer, &fell_back, &converged);
+    if (rc) return rc;
+    // true FP64 residual of the normal equations, reported with the solve
+    double rr = 0.0, rhs2 = 0.0;
+    rc = residual_f64(ctx, ctx->x.as<double>(), ctx->rhs.as<double>(), ctx->res.as<double>(), &rr);
+    if (!rc) rc = sumsq_host(ctx, ctx->rhs.as<double>(), m, &rhs2);
+    if (rc) return rc;
+    // x_1 = D^-1 (b_1 - A^T x_2) = D^-1/2 (u - B^T x_2)   (UsePCG_CPU.cpp:171-177)
+    CK(spmv_launch<double>(kEpiBacksub, ctx->it_csc.items(), ctx->it_csc.n, ctx->cp.as<int>(), ctx->ri.as<int>(),
+                           ctx->bvT.as<double>(), ctx->it_csc.cap, ctx->x.as<double>(), ctx->x1.as<double>(),
+                           ctx->u.as<double>(), nullptr, ctx->s.as<double>(), 0.0, 0, ctx->threads, ctx->stream));
+    rc = d2h(ctx, x_1, ctx->x1.as<double>(), n);
+    if (!rc) rc = d2h(ctx, x_2, ctx->x.as<double>(), m);
+    if (rc) return rc;
+    ctx->have_prev_x2 = true;
+    ctx->stats.cg_iterations = iters;
+    ctx->stats.cg_iterations_total += iters;
+    ctx->stats.ir_outer = outer;
+    ctx->stats.fell_back = fell_back;
+    ctx->stats.converged = converged;
+    ctx->stats.rel_residual = rhs2 > 0.0 ? std::sqrt(rr / rhs2) : std::sqrt(rr);
+    ctx->stats.solve_ms = now_ms() - t0;
+    ctx->stats.solves++;
+    if (!converged && !ctx->opt.fallback) return fail(ctx, HELP_E_NOT_CONVERGED, "solve: iteration cap reached");
+    return HELP_OK;
+}
+
+int help_pcg_get_stats(const help_pcg* ctx, help_pcg_stats* out) {
+    if (!ctx || !out) return HELP_E_ARG;
+    *out = ctx->stats;
+    return HELP_OK;
+}
+
+const char* help_pcg_last_error(const help_pcg* ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+int help_pcg_matvec_dev(help_pcg* ctx, int32_t op, int32_t fp32, const void* x, void* y, void* stream) {
+    if (!ctx || !x || !y) return HELP_E_ARG;
+    if (!ctx->constructed) return fail(ctx, HELP_E_ARG, "matvec: construct first");
+    if ((op == HELP_OP_ADAT || fp32) && !ctx->renewed) return fail(ctx, HELP_E_ARG, "matvec: renew first");
+    if (fp32 && ctx->opt.precision != HELP_PREC_MIXED)
+        return fail(ctx, HELP_E_ARG, "matvec: FP32 copy exists only with HELP_PREC_MIXED");
+    cudaStream_t st = stream ? (cudaStream_t)stream : ctx->stream;
+    const ItemList& icsr = fp32 ? ctx->it_csr32 : ctx->it_csr;
+    const ItemList& icsc = fp32 ? ctx->it_csc32 : ctx->it_csc;
+    if (op == HELP_OP_A || op == HELP_OP_AT) {
+        if (fp32) return fail(ctx, HELP_E_ARG, "matvec: A / A^T only in FP64");
+        const bool t = op == HELP_OP_AT;
+        const ItemList& L = t ? ctx->it_csc : ctx->it_csr;
+        CK(spmv_launch<double>(kEpiStore, L.items(), L.n, t ? ctx->cp.as<int>() : ctx->rp.as<int>(),
+                               t ? ctx->ri.as<int>() : ctx->ci.as<int>(), t ? ctx->avT.as<double>() : ctx->av.as<double>(),
+                               L.cap, (const double*)x, (double*)y, nullptr, nullptr, nullptr, 0.0, 0, ctx->threads, st));
+        return HELP_OK;
+    }
+    if (op != HELP_OP_ADAT) return fail(ctx, HELP_E_ARG, "matvec: unknown op");
+    if (fp32) {
+        CK(spmv_launch<float>(kEpiStore, icsc.items(), icsc.n, ctx->cp.as<int>(), ctx->ri.as<int>(),
+                              ctx->bvT32.as<float>(), icsc.cap, (const float*)x, ctx->t32.as<float>(), nullptr, nullptr,
+                              nullptr, 0.0, 0, ctx->threads, st));
+        CK(spmv_launch<float>(kEpiAddDelta, icsr.items(), icsr.n, ctx->rp.as<int>(), ctx->ci.as<int>(),
+                              ctx->bv32.as<float>(), icsr.cap, ctx->t32.as<float>(), (float*)y, (const float*)x,
+                              nullptr, nullptr, ctx->opt.delta, 0, ctx->threads, st));
+    } else {
+        CK(spmv_launch<double>(kEpiStore, icsc.items(), icsc.n, ctx->cp.as<int>(), ctx->ri.as<int>(),
+                               ctx->bvT.as<double>(), icsc.cap, (const double*)x, ctx->t.as<double>(), nullptr,
+                               nullptr, nullptr, 0.0, 0, ctx->threads, st));
+        CK(spmv_launch<double>(kEpiAddDelta, icsr.items(), icsr.n, ctx->rp.as<int>(), ctx->ci.as<int>(),
+                               ctx->bv.as<double>(), icsr.cap, ctx->t.as<double>(), (double*)y, (const double*)x,
+                               nullptr, nullptr, ctx->opt.delta, 0, ctx->threads, st));
+    }
+    return HELP_OK;
+}
+
+int help_pcg_matvec(help_pcg* ctx, int32_t op, const double* x, double* y) {
+    if (!ctx || !x || !y) return HELP_E_ARG;
+    if (!ctx->constructed) return fail(ctx, HELP_E_ARG, "matvec: construct first");
+    CK(cudaSetDevice(ctx->device));
+    const size_t nin = (op == HELP_OP_A) ? ctx->n : ctx->m;
+    const size_t nout = (op == HELP_OP_AT) ? ctx->n : ctx->m;
+    int rc = h2d(ctx, ctx->xacc.as<double>(), x, nin);
+    if (rc) return rc;
+    rc = help_pcg_matvec_dev(ctx, op, 0, ctx->xacc.p, ctx->res.p, nullptr);
+    if (rc) return rc;
+    return d2h(ctx, y, ctx->res.as<double>(), nout);
+}
+
+int help_pcg_precond_apply(help_pcg* ctx, const double* r, double* z) {
+    if (!ctx || !r || !z) return HELP_E_ARG;
+    if (!ctx->renewed) return fail(ctx, HELP_E_ARG, "precond: renew first");
+    CK(cudaSetDevice(ctx->device));
+    int rc = h2d(ctx, ctx->r0.as<double>(), r, ctx->m);
+    if (rc) return rc;
+    CK(vec_fill(ctx->xacc.as<double>(), 0.0, ctx->m, ctx->stream));
+    CK(vec_fill(ctx->p1.as<double>(), 0.0, ctx->m, ctx->stream));
+    CgResult res;
+    rc = run_pcg<double>(ctx, ctx->xacc.as<double>(), ctx->r0.as<double>(), 0.0, 1, 1, &res);
+    if (rc) return rc;
+    return d2h(ctx, z, ctx->p1.as<double>(), ctx->m);
+}
+
+int help_pcg_get_pivots(help_pcg* ctx, int32_t* pivots, double* diag_g, double* diag_s) {
+    if (!ctx) return HELP_E_ARG;
+    if (!ctx->renewed) return fail(ctx, HELP_E_ARG, "pivots: renew first");
+    CK(cudaSetDevice(ctx->device));
+    if (pivots && ctx->k > 0) {
+        CK(cudaMemcpyAsync(pivots, ctx->piv.p, 4 * (size_t)ctx->k, cudaMemcpyDeviceToHost, ctx->stream));
+        CK(cudaStreamSynchronize(ctx->stream));
+    }
+    int rc = HELP_OK;
+    if (diag_g) rc = d2h(ctx, diag_g, ctx->diag.as<double>(), ctx->m);
+    if (!rc && diag_s) {
+        rc = d2h(ctx, diag_s, ctx->dsinv.as<double>(), ctx->m);
+        for (int32_t i = 0; !rc && i < ctx->m; ++i) diag_s[i] = diag_s[i] != 0.0 ? 1.0 / diag_s[i] : 0.0;
+    }
+    return rc;
+}
+
+int help_pcg_cg(help_pcg* ctx, const double* b, double* x, int64_t* iters) {
+    if (!ctx || !b || !x) return HELP_E_ARG;
+    if (!ctx->renewed) return fail(ctx, HELP_E_ARG, "cg: renew first");
+    CK(cudaSetDevice(ctx->device));
+    int rc = h2d(ctx, ctx->r0.as<double>(), b, ctx->m);
+    if (rc) return rc;
+    CK(vec_fill(ctx->x.as<double>(), 0.0, ctx->m, ctx->stream));
+    CgResult res;
+    rc = run_pcg<double>(ctx, ctx->x.as<double>(), ctx->r0.as<double>(), ctx->opt.cg_tol, ctx->opt.cg_max_iter, 0, &res);
+    if (rc) return rc;
+    if (iters) *iters = res.iterations;
+    return d2h(ctx, x, ctx->x.as<double>(), ctx->m);
+}
+
+int help_adat_assemble(help_pcg* ctx, const double* w, int32_t* row_ptr, int32_t* col, double* val, int64_t* nnz) {
+    if (!ctx || !w || !row_ptr || !nnz) return HELP_E_ARG;
+    if (!ctx->constructed) return fail(ctx, HELP_E_ARG, "adat: construct first");
+    CK(cudaSetDevice(ctx->device));
+    const int m = ctx->m;
+    int rc = h2d(ctx, ctx->res.as<double>(), w, ctx->n);
+    if (rc) return rc;
+    int* cnt = ctx->cr_cnt.as<int>();
+    CK(adat_count(ctx->rp.as<int>(), ctx->ci.as<int>(), ctx->cp.as<int>(), ctx->ri.as<int>(), m, cnt, ctx->stream));
+    std::vector<int32_t> hc((size_t)m);
+    CK(cudaMemcpyAsync(hc.data(), cnt, 4 * (size_t)m, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    int64_t total = 0;
+    row_ptr[0] = 0;
+    for (int i = 0; i < m; ++i) {
+        if (hc[i] < 0) return fail(ctx, HELP_E_ARG, "adat: a row has more contributions than the assembly supports");
+        total += hc[i];
+        if (total > 2147483647LL) return fail(ctx, HELP_E_ARG, "adat: result exceeds int32 indexing");
+        row_ptr[i + 1] = (int32_t)total;
+    }
+    *nnz = total;
+    if (!col || !val) return HELP_OK;
+    CK(ctx->adat_tmp.ensure(4 * ((size_t)m + 1) + 12 * (size_t)std::max<int64_t>(total, 1) + 16));
+    int* drp = ctx->adat_tmp.as<int>();
+    int* dci = drp + m + 1 + ((m + 1) & 1);
+    double* dv = reinterpret_cast<double*>(dci + total + (total & 1));
+    CK(cudaMemcpyAsync(drp, row_ptr, 4 * ((size_t)m + 1), cudaMemcpyHostToDevice, ctx->stream));
+    CK(adat_fill(ctx->rp.as<int>(), ctx->ci.as<int>(), ctx->av.as<double>(), ctx->cp.as<int>(), ctx->ri.as<int>(),
+                 ctx->avT.as<double>(), ctx->res.as<double>(), m, drp, dci, dv, ctx->stream));
+    CK(cudaMemcpyAsync(col, dci, 4 * (size_t)total, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaMemcpyAsync(val, dv, 8 * (size_t)total, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return HELP_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,128 @@
+// Host-side state of one help_pcg context (one matrix resident on one GPU).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/help_gpu.h"
+#include "items.h"
+
+namespace help {
+
+// Growable device buffer (contents not preserved on growth).
+struct DevMem {
+    void* p = nullptr;
+    size_t bytes = 0;
+    cudaError_t ensure(size_t b) {
+        if (b == 0) b = 16;
+        if (b <= bytes) return cudaSuccess;
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+        cudaError_t e = cudaMalloc(&p, b);
+        if (e == cudaSuccess) bytes = b;
+        return e;
+    }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+    }
+    template <class T>
+    T* as() const {
+        return static_cast<T*>(p);
+    }
+};
+
+struct ItemList {
+    DevMem buf;
+    int32_t n = 0;
+    int32_t cap = 0;
+    const int4* items() const { return buf.as<int4>(); }
+};
+
+// Results the persistent CG kernel leaves behind.
+struct CgOut {
+    long long iterations;
+    double rr0;
+    double rr;
+    int converged;
+    int status;
+};
+
+// Device control block: barrier words, status, CG outputs, top-k state.
+struct Ctrl {
+    unsigned int bar_count;
+    unsigned int bar_gen;
+    int status;
+    int pad;
+    CgOut cg;
+    // radix top-k selection state
+    unsigned long long prefix;     // selected high bits of the threshold key
+    unsigned long long mask;       // bits decided so far
+    int remaining;                 // how many still to take at/below the prefix
+    int n_greater;                 // rows strictly above the final threshold
+    int scratch[2];
+};
+
+constexpr int kCapF64 = 2048;   // nonzeros per SpMV work item (FP64 staging: 32 KB)
+constexpr int kCapF32 = 4096;   // (FP32 staging: 32 KB)
+constexpr int kTopkBins = 256;
+
+}  // namespace help
+
+struct help_pcg {
+    help_pcg_options opt;
+    int device = 0;
+    int num_sms = 0;
+    cudaStream_t stream = nullptr;
+    std::string err;
+
+    // matrix
+    int32_t m = 0, n = 0;
+    int64_t nnz = 0;
+    bool constructed = false;
+    bool renewed = false;
+    std::vector<int32_t> h_rp, h_cp;  // host copies of the pointers (planning)
+    help::DevMem rp, ci, av;          // CSR(A), original values
+    help::DevMem cp, ri, avT;         // CSR(A^T) = CSC(A), original values
+    help::DevMem bv, bvT;             // B = A D^-1/2 (FP64)
+    help::DevMem bv32, bvT32;         // B in FP32 (mixed precision)
+    help::ItemList it_csr, it_csc;    // FP64 plans
+    help::ItemList it_csr32, it_csc32;  // FP32 plans
+
+    // renew state
+    int32_t k = 0;
+    int64_t nnz_c = 0;
+    help::DevMem d, s, diag, dsinv, dsinv32, piv, pivpos;
+    help::DevMem keys, hist, flags, scan_tmp;
+    help::DevMem bp_ptr, bp_c, bp_v;      // per column of A: pivot entries (c, B value)
+    help::DevMem cr_cnt;                  // per row: entries of G[i,P]
+    help::DevMem c_rp, c_ci, c_v, c_v32;  // C = G[non-pivot rows, P], CSR over all m rows
+    help::DevMem ct_rp, ct_ci, ct_v, ct_v32, ct_blk;  // C^T, CSR over k rows
+    help::ItemList it_c, it_ct, it_c32, it_ct32;
+    help::DevMem g11, W, lwork;           // pivot block, its inverse, factor workspace
+    std::vector<int32_t> h_tmp;
+    int32_t dense_regularised = 0;
+
+    // vectors
+    help::DevMem x, r0, r1, z, p0, p1, q, t, a, w;         // FP64 CG
+    help::DevMem x32, r032, r132, z32, p032, p132, q32, t32;  // FP32 CG
+    help::DevMem u, rhs, b1, b2, x1, x2, res, xacc;         // solve-level FP64 vectors
+    help::DevMem partials;
+    help::DevMem ctrl;
+    help::DevMem adat_tmp;
+
+    // host staging (pinned)
+    double* h_stage = nullptr;
+    size_t h_stage_elems = 0;
+
+    const double* last_d = nullptr;
+    bool have_prev_x2 = false;
+    help_pcg_stats stats{};
+    int coop_blocks_f64 = 0, coop_blocks_f32 = 0;
+    int threads = 512;
+};

@@ -1,0 +1,165 @@
+// Host-callable launchers of the device kernels (one declaration list for
+// api.cu).  All launches are asynchronous on the given stream.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "common.cuh"
+
+namespace help {
+
+struct TopkStateDev {
+    unsigned long long prefix;  // high bits of the threshold key decided so far
+    unsigned long long mask;
+    int remaining;              // rows still to take at or below the prefix
+    int n_greater;              // rows strictly above the threshold
+};
+
+struct CgOutDev {
+    long long iterations;
+    double rr0;
+    double rr;
+    int converged;
+    int status;
+    int final_buf;
+    int pad;
+};
+
+// Device control block (one per context).
+struct DevCtrl {
+    unsigned int bar_count;
+    unsigned int bar_gen;
+    int status;
+    int regularised;
+    CgOutDev cg;
+    TopkStateDev topk;
+    int totals[8];
+};
+
+template <class V>
+struct PcgArgs {
+    int m, n, k, cap;
+    const int4* csr_items;
+    int n_csr;
+    const int* rp;
+    const int* ci;
+    const V* bv;
+    const int4* csc_items;
+    int n_csc;
+    const int* cp;
+    const int* ri;
+    const V* bvT;
+    const int4* c_items;
+    int n_c;
+    const int* c_rp;
+    const int* c_ci;
+    const V* c_v;
+    const int4* ct_items;
+    int n_ct;
+    const int* ct_rp;
+    const int* ct_ci;
+    const V* ct_v;
+    const int* piv;
+    const int* pivpos;
+    const double* W;
+    const V* dsinv;
+    double delta;
+    double tol2;
+    long long max_iter;
+    V* x;
+    V* r0;
+    V* r1;
+    V* z;
+    V* p0;
+    V* p1;
+    V* q;
+    V* t;
+    double* a;
+    double* w;
+    double* part;  // 3 * gridDim doubles
+    int precond_only;  // stop after the first preconditioner application (z in p1)
+    GridBarrier bar;
+    CgOutDev* out;
+};
+
+template <class V>
+cudaError_t pcg_configure(int threads, size_t smem, int* blocks_per_sm);
+template <class V>
+cudaError_t pcg_launch(const PcgArgs<V>& args, int blocks, int threads, size_t smem, cudaStream_t stream);
+
+// ---- standalone SpMV over items (vec.cu)
+enum SpmvEpi {
+    kEpiStore = 0,     // y[row] = s
+    kEpiRhs = 1,       // y[row] = s - aux[row]                (A D^-1 b1 - b2)
+    kEpiBacksub = 2,   // y[row] = s2[row] * (aux[row] - s)    (D^-1 (b1 - A^T x2))
+    kEpiResid = 3,     // y[row] = aux[row] - (s + delta * aux2[row])  (rhs - G x)
+    kEpiAddDelta = 4   // y[row] = s + delta * aux[row]
+};
+template <class V>
+cudaError_t spmv_launch(int epi, const int4* items, int n_items, const int* ptr, const int* idx, const V* val,
+                        int cap, const V* x, V* y, const V* aux, const V* aux2, const double* s2, double delta,
+                        int blocks, int threads, cudaStream_t stream);
+
+// ---- vector kernels (vec.cu)
+cudaError_t vec_scale_mul(const double* a, const double* b, double* out, int64_t n, cudaStream_t st);  // out = a*b
+cudaError_t vec_to_f32(const double* a, float* out, int64_t n, cudaStream_t st);
+cudaError_t vec_add_f32(double* x, const float* e, int64_t n, cudaStream_t st);  // x += e
+cudaError_t vec_to_f32_scaled(const double* a, double scale, float* out, int64_t n, cudaStream_t st);
+cudaError_t vec_add_f32_scaled(double* x, const float* e, double scale, int64_t n, cudaStream_t st);
+cudaError_t vec_fill(double* x, double v, int64_t n, cudaStream_t st);
+cudaError_t vec_fill_f32(float* x, float v, int64_t n, cudaStream_t st);
+// Deterministic sum of squares into out[0] (uses `part` of >= 1024 doubles).
+cudaError_t vec_sumsq(const double* x, int64_t n, double* part, double* out, cudaStream_t st);
+
+// ---- renew pipeline (renew.cu)
+// s = d^-1/2 (status <- numeric error if some d_j is not positive and finite)
+cudaError_t renew_inv_sqrt(const double* d, double* s, int n, int* status, cudaStream_t st);
+// B = A diag(s) in both layouts (FP32 copies when bv32 / bvT32 are not null)
+// and diag = rowsum(B .* B) + delta.
+cudaError_t renew_scale_values(const double* s, const int* rp, const int* ci, const double* av, double* bv,
+                               float* bv32, const int* cp, const double* avT, double* bvT, float* bvT32,
+                               double* diag, double delta, int m, int n, int64_t nnz, cudaStream_t st);
+// Top-k rows by key (diag >= 0); pivots ascending in piv[0..k), pivpos[m] = position or -1.
+// flags: 3*m ints of scratch.
+cudaError_t topk_select(const double* diag, int m, int k, unsigned long long* keys, unsigned int* hist,
+                        int* flags, int* scan_tmp, TopkStateDev* tst, int* status, int* piv, int* pivpos,
+                        cudaStream_t st);
+size_t scan_tmp_elems(int64_t n);
+// Exclusive scan of n int32 (in place allowed); writes the total to *total_dev if not null.
+cudaError_t exclusive_scan(const int* in, int* out, int64_t n, int* tmp, int* total_dev, cudaStream_t st);
+cudaError_t pivot_lists_count(const int* cp, const int* ri, const int* pivpos, int n, int* cnt, cudaStream_t st);
+cudaError_t pivot_lists_fill(const int* cp, const int* ri, const double* bvT, const int* pivpos, int n,
+                             const int* bp_ptr, int* bp_c, double* bp_v, cudaStream_t st);
+size_t gcols_smem_bytes(int k);
+int gcols_warps(int k);
+// Row-wise G[i, P] (pass 0: counts per non-pivot row into cnt; pass 1: fill C rows / dense G11).
+cudaError_t gcols_rows(int pass, const int* rp, const int* ci, const double* bv, const int* bp_ptr, const int* bp_c,
+                       const double* bp_v, const int* pivpos, int m, int k, double delta, int* cnt, const int* c_rp,
+                       int* c_ci, double* c_v, double* g11, int num_sms, cudaStream_t st);
+// Deterministic transpose of C (m rows, k columns): per-block counts, scan, fill.
+int ct_rows_per_block();
+cudaError_t ct_count(const int* c_rp, const int* c_ci, int m, int k, int* blk_cnt, cudaStream_t st);
+cudaError_t ct_fill(const int* c_rp, const int* c_ci, const double* c_v, int m, int k, const int* blk_off,
+                    int* ct_ci, double* ct_v, cudaStream_t st);
+cudaError_t ct_row_ptr(const int* blk_off, int k, int nblk, const int* total_dev, int* ct_rp, cudaStream_t st);
+// Copy values to FP32.
+cudaError_t vals_to_f32(const double* a, float* out, int64_t n, cudaStream_t st);
+// D_S^-1 for non-pivot rows (1/diag when k == 0); 0 for pivot rows.
+cudaError_t schur_diag(const int* c_rp, const int* c_ci, const double* c_v, const double* W, const double* diag,
+                       const int* pivpos, int m, int k, double floor_rel, double* dsinv, float* dsinv32,
+                       cudaStream_t st);
+
+// ---- dense pivot block (dense.cu): W = G11^-1 through Cholesky; returns the
+// number of regularised pivots in *regularised (device int).
+size_t dense_work_elems(int k);
+cudaError_t dense_spd_inverse(double* g11, double* W, double* work, int k, int* regularised, cudaStream_t st);
+
+// ---- explicit A diag(w) A^T (adat.cu)
+cudaError_t adat_count(const int* rp, const int* ci, const int* cp, const int* ri, int m, int* cnt,
+                       cudaStream_t st);
+cudaError_t adat_fill(const int* rp, const int* ci, const double* av, const int* cp, const int* ri,
+                      const double* avT, const double* wv, int m, const int* out_rp, int* out_ci, double* out_v,
+                      cudaStream_t st);
+
+}  // namespace help

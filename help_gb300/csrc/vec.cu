@@ -1,0 +1,162 @@
+// Standalone SpMV launches (the two passes of one A D^-1 A^T v, the
+// right-hand side A D^-1 b_1 - b_2 and the back-substitution
+// D^-1 (b_1 - A^T x_2) of UsePCG_CPU.cpp:103-177, the FP64 residual of the
+// refinement loop) and small vector kernels.
+#include "common.cuh"
+#include "kernels.h"
+#include "spmv.cuh"
+
+namespace help {
+
+namespace {
+
+template <class V, int EPI>
+__global__ void __launch_bounds__(512) k_spmv(const int4* __restrict__ items, int n_items, const int* __restrict__ ptr,
+                                              const int* __restrict__ idx, const V* __restrict__ val, int cap,
+                                              const V* __restrict__ x, V* __restrict__ y, const V* __restrict__ aux,
+                                              const V* __restrict__ aux2, const double* __restrict__ s2, double delta) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    V* s_val = reinterpret_cast<V*>(smem_raw);
+    V* s_x = s_val + cap;
+    __shared__ double red[32];
+    spmv_items<V>(
+        items, n_items, blockIdx.x, gridDim.x, ptr, idx, val, cap, [&](int c) { return ld_ro(x + c); },
+        [&](int row, V s) {
+            if (EPI == kEpiStore) {
+                y[row] = s;
+            } else if (EPI == kEpiRhs) {
+                y[row] = s - aux[row];
+            } else if (EPI == kEpiBacksub) {
+                y[row] = (V)(s2[row] * ((double)aux[row] - (double)s));
+            } else if (EPI == kEpiResid) {
+                y[row] = aux[row] - fma_t((V)delta, aux2[row], s);
+            } else {
+                y[row] = fma_t((V)delta, aux[row], s);
+            }
+        },
+        s_val, s_x, red);
+}
+
+__global__ void k_mul(const double* __restrict__ a, const double* __restrict__ b, double* __restrict__ out, int64_t n) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        out[i] = a[i] * b[i];
+}
+__global__ void k_to_f32(const double* __restrict__ a, float* __restrict__ out, int64_t n) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        out[i] = (float)a[i];
+}
+__global__ void k_add_f32(double* __restrict__ x, const float* __restrict__ e, int64_t n) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        x[i] += (double)e[i];
+}
+__global__ void k_to_f32_scaled(const double* __restrict__ a, double scale, float* __restrict__ out, int64_t n) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        out[i] = (float)(a[i] * scale);
+}
+__global__ void k_add_f32_scaled(double* __restrict__ x, const float* __restrict__ e, double scale, int64_t n) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        x[i] = fma((double)e[i], scale, x[i]);
+}
+__global__ void k_fill(double* __restrict__ x, double v, int64_t n) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        x[i] = v;
+}
+__global__ void k_fill_f32(float* __restrict__ x, float v, int64_t n) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        x[i] = v;
+}
+__global__ void k_sumsq_part(const double* __restrict__ x, int64_t n, double* __restrict__ part) {
+    __shared__ double red[32];
+    double s = 0.0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        s = fma(x[i], x[i], s);
+    s = block_sum(s, red);
+    if (threadIdx.x == 0) part[blockIdx.x] = s;
+}
+__global__ void k_sum_parts(const double* __restrict__ part, int np, double* __restrict__ out) {
+    __shared__ double red[32];
+    double s = 0.0;
+    for (int i = threadIdx.x; i < np; i += blockDim.x) s += part[i];
+    s = block_sum(s, red);
+    if (threadIdx.x == 0) *out = s;
+}
+
+inline int grid_for(int64_t n, int threads) {
+    int64_t b = (n + threads - 1) / threads;
+    if (b < 1) b = 1;
+    if (b > 4096) b = 4096;
+    return (int)b;
+}
+
+}  // namespace
+
+template <class V>
+cudaError_t spmv_launch(int epi, const int4* items, int n_items, const int* ptr, const int* idx, const V* val, int cap,
+                        const V* x, V* y, const V* aux, const V* aux2, const double* s2, double delta, int blocks,
+                        int threads, cudaStream_t stream) {
+    if (n_items <= 0) return cudaSuccess;
+    const size_t smem = spmv_smem_bytes<V>(cap);
+    if (blocks <= 0 || blocks > n_items) blocks = n_items;
+    cudaError_t e = cudaSuccess;
+#define HELP_SPMV_CASE(E)                                                                                     \
+    case E:                                                                                                   \
+        e = cudaFuncSetAttribute(k_spmv<V, E>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);       \
+        if (e != cudaSuccess) return e;                                                                       \
+        k_spmv<V, E><<<blocks, threads, smem, stream>>>(items, n_items, ptr, idx, val, cap, x, y, aux, aux2, s2, delta); \
+        break;
+    switch (epi) {
+        HELP_SPMV_CASE(kEpiStore)
+        HELP_SPMV_CASE(kEpiRhs)
+        HELP_SPMV_CASE(kEpiBacksub)
+        HELP_SPMV_CASE(kEpiResid)
+        HELP_SPMV_CASE(kEpiAddDelta)
+        default:
+            return cudaErrorInvalidValue;
+    }
+#undef HELP_SPMV_CASE
+    return cudaGetLastError();
+}
+
+template cudaError_t spmv_launch<double>(int, const int4*, int, const int*, const int*, const double*, int,
+                                         const double*, double*, const double*, const double*, const double*, double,
+                                         int, int, cudaStream_t);
+template cudaError_t spmv_launch<float>(int, const int4*, int, const int*, const int*, const float*, int, const float*,
+                                        float*, const float*, const float*, const double*, double, int, int,
+                                        cudaStream_t);
+
+cudaError_t vec_scale_mul(const double* a, const double* b, double* out, int64_t n, cudaStream_t st) {
+    k_mul<<<grid_for(n, 256), 256, 0, st>>>(a, b, out, n);
+    return cudaGetLastError();
+}
+cudaError_t vec_to_f32(const double* a, float* out, int64_t n, cudaStream_t st) {
+    k_to_f32<<<grid_for(n, 256), 256, 0, st>>>(a, out, n);
+    return cudaGetLastError();
+}
+cudaError_t vec_add_f32(double* x, const float* e, int64_t n, cudaStream_t st) {
+    k_add_f32<<<grid_for(n, 256), 256, 0, st>>>(x, e, n);
+    return cudaGetLastError();
+}
+cudaError_t vec_to_f32_scaled(const double* a, double scale, float* out, int64_t n, cudaStream_t st) {
+    k_to_f32_scaled<<<grid_for(n, 256), 256, 0, st>>>(a, scale, out, n);
+    return cudaGetLastError();
+}
+cudaError_t vec_add_f32_scaled(double* x, const float* e, double scale, int64_t n, cudaStream_t st) {
+    k_add_f32_scaled<<<grid_for(n, 256), 256, 0, st>>>(x, e, scale, n);
+    return cudaGetLastError();
+}
+cudaError_t vec_fill(double* x, double v, int64_t n, cudaStream_t st) {
+    k_fill<<<grid_for(n, 256), 256, 0, st>>>(x, v, n);
+    return cudaGetLastError();
+}
+cudaError_t vec_fill_f32(float* x, float v, int64_t n, cudaStream_t st) {
+    k_fill_f32<<<grid_for(n, 256), 256, 0, st>>>(x, v, n);
+    return cudaGetLastError();
+}
+cudaError_t vec_sumsq(const double* x, int64_t n, double* part, double* out, cudaStream_t st) {
+    const int nb = 1024;
+    k_sumsq_part<<<nb, 256, 0, st>>>(x, n, part);
+    k_sum_parts<<<1, 1024, 0, st>>>(part, nb, out);
+    return cudaGetLastError();
+}
+
+}  // namespace help

@@ -1,0 +1,145 @@
+/*
+ * help_gpu.h -- C ABI of libhelp_gpu.so, the GB300 normal-equations backend.
+ *
+ * The reference (Tian-Xie/HELP) selects its normal-equations backend at link
+ * time through four C++ functions declared in LP.h:157-160 and implemented
+ * for the PCG backend in UsePCG_CPU.cpp:26-183 + PCG.cpp:38-395.  This
+ * library provides the same four operations as plain C entry points (no
+ * globals, no torch types: plain pointers, sizes and an opaque context) so a
+ * C++ shim (help_gb300/csrc/UsePCG_GPU.cpp) can re-export them under the
+ * reference's own names, and any FFI can bind them directly.
+ *
+ * Boundary contract (same as the reference's):
+ *   - all vectors passed to construct/renew/solve are HOST arrays owned by the
+ *     caller; the library keeps its own device copies of A and all scratch;
+ *   - d is D = X^-1 Z itself (not inverted);
+ *   - solve writes x_1 (n) and x_2 (m) in full;
+ *   - single-threaded caller, no re-entrancy on one context.
+ * Every entry point returns HELP_OK (0) or a negative HELP_E* code; the
+ * reference's backends exit() on fatal errors instead (Helper.cpp:24-35), the
+ * UsePCG_GPU.cpp shim keeps that behaviour.
+ */
+#ifndef HELP_GPU_H
+#define HELP_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+    HELP_OK = 0,
+    HELP_E_ARG = -1,         /* bad argument or call order                        */
+    HELP_E_CUDA = -2,        /* CUDA runtime error (message via help_pcg_last_error) */
+    HELP_E_NOMEM = -3,       /* device or host allocation failed                  */
+    HELP_E_NUMERIC = -4,     /* non-positive / non-finite d, breakdown, NaN        */
+    HELP_E_TIMEOUT = -5,     /* a device-side wait ran past its limit              */
+    HELP_E_NOT_CONVERGED = -6 /* iteration cap hit (only when fallback is disabled) */
+};
+
+enum {
+    HELP_PREC_FP64 = 0,      /* plain FP64 PCG: the drop-in form                      */
+    HELP_PREC_MIXED = 1      /* FP32 CG inside FP64 iterative refinement              */
+};
+
+typedef struct help_pcg help_pcg;  /* opaque: one matrix resident on one GPU */
+
+typedef struct help_pcg_options {
+    int32_t device;          /* CUDA device ordinal                                     */
+    int32_t pivots;          /* k, partial-Cholesky pivot count (reference: 10, PCG.h:20) */
+    int32_t precision;       /* HELP_PREC_FP64 or HELP_PREC_MIXED                        */
+    double cg_tol;           /* stop when ||r|| < cg_tol*||r0|| (reference 1e-20, PCG.h:19) */
+    int64_t cg_max_iter;     /* iteration cap per CG run (the reference has none)         */
+    double delta;            /* regularisation: solves (A D^-1 A^T + delta I) (ref: 0)   */
+    /* mixed precision */
+    double ir_tol;           /* FP64 normal-equation residual target ||r||/||rhs||      */
+    int32_t ir_max_outer;    /* refinement steps before falling back to FP64 PCG        */
+    double inner_tol;        /* relative residual reduction asked of each FP32 CG run   */
+    int64_t inner_max_iter;  /* cap per FP32 CG run                                     */
+    /* warm start / learned correction */
+    int32_t warm_start;      /* 1: start CG from the previous solve's x_2 of this renew */
+    int32_t fallback;        /* 1: on cap or failed FP64 check, redo with plain FP64 PCG */
+    int32_t threads;         /* persistent-kernel block size (0 = default)              */
+} help_pcg_options;
+
+typedef struct help_pcg_stats {
+    int64_t cg_iterations;       /* last solve: all CG iterations (inner + fallback)  */
+    int64_t cg_iterations_total; /* since construct                                   */
+    int32_t ir_outer;            /* last solve: refinement steps (mixed)              */
+    int32_t fell_back;           /* last solve: 1 if plain FP64 PCG had to finish it   */
+    int32_t converged;           /* last solve: stopping rule met                      */
+    int32_t pivots;              /* k actually used                                    */
+    double rel_residual;         /* last solve: FP64 ||rhs - G x_2|| / ||rhs||         */
+    double renew_ms, solve_ms;   /* last renew / solve wall time                       */
+    int64_t nnz_c;               /* entries of the pivot-column block G[:,P] (non-pivot rows) */
+    int32_t solves, renews;
+} help_pcg_stats;
+
+/* Fills *opt with the defaults (FP64, k = 10, cg_tol = 1e-20 as the reference). */
+void help_pcg_default_options(help_pcg_options* opt);
+
+/* Creates a context bound to opt->device; no matrix yet. */
+int help_pcg_create(const help_pcg_options* opt, help_pcg** out);
+/* Frees the context (calls help_pcg_destruct if needed). */
+void help_pcg_free(help_pcg* ctx);
+
+/* LinearEquation_Construct (UsePCG_CPU.cpp:26-68): A (m x n) given column-wise
+ * (CSC, zero-based, rows sorted inside columns).  Uploads A once as both
+ * CSC and CSR and plans the SpMV work partition. */
+int help_pcg_construct(help_pcg* ctx, int32_t m, int32_t n, const int32_t* col_ptr,
+                       const int32_t* row_ind, const double* val);
+
+/* RenewLinearEquation (UsePCG_CPU.cpp:78-80; the reference rebuilds its
+ * preconditioner inside every solve instead, PCG.cpp:301 -> :38-177):
+ * uploads d, forms B = A D^-1/2, picks the k pivots, builds G[:,P], factors
+ * the pivot block and the Schur diagonal.  Call once per interior-point
+ * iteration, before the solves that use this d. */
+int help_pcg_renew(help_pcg* ctx, const double* d);
+
+/* SolveLinearEquation (UsePCG_CPU.cpp:91-183):
+ *   [D A^T; A 0] [x_1; x_2] = [b_1; b_2]
+ *   (A D^-1 A^T) x_2 = A D^-1 b_1 - b_2,   x_1 = D^-1 (b_1 - A^T x_2)
+ * d must be the array last passed to help_pcg_renew (renews if it is not). */
+int help_pcg_solve(help_pcg* ctx, const double* d, const double* b_1, const double* b_2,
+                   double* x_1, double* x_2);
+
+/* LinearEquation_Destruct (UsePCG_CPU.cpp:70-75): releases the device matrix. */
+int help_pcg_destruct(help_pcg* ctx);
+
+int help_pcg_get_stats(const help_pcg* ctx, help_pcg_stats* out);
+const char* help_pcg_last_error(const help_pcg* ctx);
+
+/* ---- building blocks of the path, exposed for parity tests and the isolated
+ * ADA^T v benchmark.  Host arrays unless the name ends in _dev. ---- */
+
+enum { HELP_OP_A = 0, HELP_OP_AT = 1, HELP_OP_ADAT = 2 };
+
+/* y = A x (CSRMV_N, Helper.cpp:57-68), y = A^T x (CSRMV_T, Helper.cpp:71-81)
+ * or y = (A D^-1 A^T + delta I) x (PCG.cpp:346-358), D from the last renew. */
+int help_pcg_matvec(help_pcg* ctx, int32_t op, const double* x, double* y);
+/* Same on device pointers, on `stream` (a cudaStream_t, NULL = default);
+ * fp32 != 0 runs the FP32 copy of B (x, y are then float*). */
+int help_pcg_matvec_dev(help_pcg* ctx, int32_t op, int32_t fp32, const void* x, void* y,
+                        void* stream);
+/* z = M^-1 r with the last renew's partial-Cholesky preconditioner
+ * (Preconditioner, PCG.cpp:183-196), vectors in the original row order. */
+int help_pcg_precond_apply(help_pcg* ctx, const double* r, double* z);
+/* Pivot rows (ascending, k of them), diag(A D^-1 A^T) and the Schur diagonal
+ * D_S used for non-pivot rows (PCG.cpp:41-46, :100-102). Any pointer may be NULL. */
+int help_pcg_get_pivots(help_pcg* ctx, int32_t* pivots, double* diag_g, double* diag_s);
+/* One PCG run on (A D^-1 A^T + delta I) x = b from x = 0 with the current
+ * preconditioner (ConjugateGradient, PCG.cpp:296-395); returns iterations in *iters. */
+int help_pcg_cg(help_pcg* ctx, const double* b, double* x, int64_t* iters);
+
+/* Explicit A diag(w) A^T, upper triangle incl. diagonal, CSR with columns
+ * sorted in each row (ADAt_Allocate + ADAt_Calc, Helper.cpp:215-377; the
+ * reference keeps discovery order inside a row).  Two-call protocol: with
+ * col == NULL only *nnz is returned; then pass arrays of that size. */
+int help_adat_assemble(help_pcg* ctx, const double* w, int32_t* row_ptr, int32_t* col, double* val,
+                       int64_t* nnz);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,130 @@
+/*
+ * help_lp.h -- host-side C ABI of libhelp_lp.so: seeded LP instance generators,
+ * the MPS writer that feeds the same instances to the reference program, and
+ * the homogeneous self-dual (HSD) interior-point driver that calls a
+ * normal-equations backend through the four entry points the reference's
+ * HSDSolver.cpp calls (LP.h:157-160).
+ *
+ * Everything here is plain C: int32 indices, double values, caller-visible
+ * arrays allocated with malloc and released by help_lp_free().
+ */
+#ifndef HELP_LP_H
+#define HELP_LP_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Instance families (the five benchmark configurations map onto these). */
+enum {
+    HELP_LP_RANDOM = 0,   /* k nonzeros per column at uniform-random distinct rows   */
+    HELP_LP_ZIPF = 1,     /* k nonzeros per column, rows from a Zipf rank law        */
+    HELP_LP_MCF = 2,      /* multicommodity flow on a 4-neighbour grid graph         */
+    HELP_LP_BLOCK = 3     /* block-angular: diagonal random blocks + linking rows    */
+};
+
+typedef struct help_lp_spec {
+    int32_t kind;
+    int32_t m, n, nnz_per_col;      /* RANDOM / ZIPF                                */
+    double zipf_s;                  /* ZIPF: exponent of the rank law               */
+    int32_t zipf_offset;            /* ZIPF: rank offset that flattens the head     */
+    int32_t grid, commodities;      /* MCF: grid side, number of commodities        */
+    int32_t pairs_per_commodity;    /* MCF: source/sink pairs routed per commodity  */
+    int32_t blocks, block_rows, block_cols, link_rows;  /* BLOCK                    */
+    double link_prob;               /* BLOCK: P(column appears in a linking row)    */
+} help_lp_spec;
+
+/*
+ * A standard-form LP  min c^T x  s.t.  A x = b, x >= 0, stored column-major
+ * (CSC, row indices sorted inside each column).  All values lie on a 1e-6
+ * decimal grid so the MPS text written by help_lp_write_mps() parses back to
+ * bit-identical doubles.  Inequality rows (MCF capacity rows) are already
+ * closed with slack columns appended after the structural columns, in row
+ * order, exactly as the reference's bound/row standardisation does
+ * (Crushing.cpp:71-99); n_struct counts the columns before the slacks and
+ * row_type[i] is 'E' or 'L' for the MPS writer.
+ */
+typedef struct help_lp {
+    int32_t m, n, n_struct;
+    int64_t nnz;
+    int32_t* col_ptr;   /* n + 1   */
+    int32_t* row_ind;   /* nnz     */
+    double* val;        /* nnz     */
+    double* b;          /* m       */
+    double* c;          /* n       */
+    char* row_type;     /* m       */
+} help_lp;
+
+/* Returns 0 on success, a negative code on bad parameters or allocation failure. */
+int help_lp_generate(const help_lp_spec* spec, uint64_t seed, help_lp* out);
+void help_lp_free(help_lp* lp);
+
+/* Writes the instance (structural columns only, inequality rows as 'L') in
+ * the fixed-column MPS layout the reference parser reads (MPSRead.cpp:18,
+ * card positions 4/14/24).  Returns 0 on success. */
+int help_lp_write_mps(const help_lp* lp, const char* path);
+
+/* Row-major copy (CSR, column indices sorted inside each row) of a CSC matrix. */
+int help_csc_to_csr(int32_t m, int32_t n, const int32_t* col_ptr, const int32_t* row_ind,
+                    const double* val, int32_t* row_ptr, int32_t* col_ind, double* val_out);
+
+/* ------------------------------------------------------------------------ */
+/* HSD interior-point driver                                                 */
+/* ------------------------------------------------------------------------ */
+
+/*
+ * The four normal-equations entry points, as function pointers, so one
+ * driver binary can run against any backend (the GPU library, or the CPU
+ * restatement used as the measured baseline).  Semantics follow the
+ * reference boundary (LP.h:157-160, UsePCG_CPU.cpp:26-183):
+ *   construct(ctx, m, n, csc...)  -- LinearEquation_Construct
+ *   renew(ctx, d)                 -- RenewLinearEquation, d = X^-1 Z (not inverted)
+ *   solve(ctx, d, b1, b2, x1, x2) -- SolveLinearEquation for
+ *                                    [D A^T; A 0][x1; x2] = [b1; b2]
+ *   destruct(ctx)                 -- LinearEquation_Destruct
+ * Each returns 0 on success.
+ */
+typedef struct help_ne_backend {
+    void* ctx;
+    int (*construct)(void* ctx, int32_t m, int32_t n, const int32_t* col_ptr,
+                     const int32_t* row_ind, const double* val);
+    int (*renew)(void* ctx, const double* d);
+    int (*solve)(void* ctx, const double* d, const double* b_1, const double* b_2,
+                 double* x_1, double* x_2);
+    int (*destruct)(void* ctx);
+} help_ne_backend;
+
+typedef struct help_hsd_options {
+    int32_t max_iterations;     /* reference: Max_Iterations = 10000 (LP.h:86)   */
+    double gap_tol;             /* reference: 1e-8 (LP.h:89)                     */
+    double pinf_tol, dinf_tol;  /* reference: 1e-8 (LP.h:90-91)                  */
+    int32_t verbose;            /* print the reference's per-iteration table     */
+    /* Optional per-iteration callback (iteration, primal obj, dual obj, rel gap,
+     * primal infeasibility, dual infeasibility); may be NULL. */
+    void (*on_iter)(void* user, int32_t iter, const double* stats6);
+    void* user;
+} help_hsd_options;
+
+typedef struct help_hsd_result {
+    int32_t status;             /* 0 OK, 1 stalled, 2 iteration limit, 3 unknown (LP.h:163-167) */
+    int32_t iterations;         /* rows of the reference table printed (Iter + 1 at exit) */
+    int32_t solves;             /* normal-equation solves issued                 */
+    int32_t renews;
+    double primal_obj, dual_obj, rel_gap, primal_infeas, dual_infeas;
+    double tau, kappa;
+    double wall_s, backend_s;   /* total and time spent inside backend calls     */
+} help_hsd_result;
+
+void help_hsd_default_options(help_hsd_options* opt);
+
+/* Runs the HSD method (the reference's HSD_Main, HSDSolver.cpp:869-883) on an
+ * all-lower-bounded standard-form LP.  x_out (n) / y_out (m) may be NULL. */
+int help_hsd_solve(const help_lp* lp, const help_ne_backend* be, const help_hsd_options* opt,
+                   help_hsd_result* res, double* x_out, double* y_out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,175 @@
+"""GPU parity: every building block of the path through the C ABI against the
+CPU oracle (a restatement of the reference pinned to the reference itself in
+test_oracle_pin.py).
+
+Tolerances: FP64 kernels agree with the oracle to 1e-12 relative (summation
+order differs); iterative solves are compared after both reach the same
+stopping rule, to 1e-8 relative; index work (pivots, ADA^T pattern) is exact.
+"""
+import numpy as np
+import pytest
+
+from help_gb300 import backend, lp as L
+from oracle import bindings as ob
+
+pytestmark = pytest.mark.gpu
+
+
+def rel(a, b):
+    return np.linalg.norm(np.asarray(a) - np.asarray(b)) / max(np.linalg.norm(b), 1e-300)
+
+
+CASES = {
+    "random": lambda: L.generate(L.spec_random(400, 1200, 5), 3),
+    "zipf": lambda: L.generate(L.spec_zipf(3000, 12000, 6, 1.3, 70), 4),
+    "block": lambda: L.generate(L.spec_block(4, 300, 1200, 5, 40, 0.05), 5),
+    "mcf": lambda: L.generate(L.spec_mcf(12, 3, 3), 6),
+}
+
+
+@pytest.fixture(scope="module", params=sorted(CASES))
+def case(request):
+    lp = CASES[request.param]()
+    rng = np.random.default_rng(11)
+    d = np.exp(rng.uniform(-6, 6, lp.n))
+    return request.param, lp, d, rng
+
+
+def test_mkl_known_answer():
+    # [1 0 2; 0 3 0; 4 0 5] * [3 5 7]^T = [17 15 47]^T (Main.cpp:19-35)
+    col_ptr = np.array([0, 2, 3, 5], np.int32)
+    row_ind = np.array([0, 2, 1, 0, 2], np.int32)
+    val = np.array([1.0, 4.0, 3.0, 2.0, 5.0])
+    with backend.GpuNormalEquations(pivots=1) as g:
+        g.LinearEquation_Construct(m=3, n=3, col_ptr=col_ptr, row_ind=row_ind, val=val)
+        y = g.matvec("A", np.array([3.0, 5.0, 7.0]))
+    assert np.array_equal(y, [17.0, 15.0, 47.0])
+
+
+def test_spmv_and_adat(case):
+    name, lp, d, rng = case
+    rp, ci, v = lp.csr()
+    with backend.GpuNormalEquations(pivots=8) as g:
+        g.LinearEquation_Construct(lp)
+        x = rng.standard_normal(lp.n)
+        w = rng.standard_normal(lp.m)
+        assert rel(g.matvec("A", x), ob.csrmv_n(rp, ci, v, x, lp.m, lp.n)) < 1e-13
+        assert rel(g.matvec("AT", w), ob.csrmv_t(rp, ci, v, w, lp.m, lp.n)) < 1e-13
+        g.RenewLinearEquation(d)
+        y = g.matvec("ADAT", w)
+        t = ob.csrmv_t(rp, ci, v, w, lp.m, lp.n) / d
+        assert rel(y, ob.csrmv_n(rp, ci, v, t, lp.m, lp.n)) < 1e-11
+
+
+@pytest.mark.parametrize("k", [0, 1, 10, 64])
+def test_pivots_diag_schur_precond(case, k):
+    name, lp, d, rng = case
+    rp, ci, v = lp.csr()
+    with backend.GpuNormalEquations(pivots=k) as g:
+        g.LinearEquation_Construct(lp)
+        g.RenewLinearEquation(d)
+        piv, dg, ds = g.pivots()
+        dg_ref = ob.diag_adat(rp, ci, v, d, lp.m)
+        assert rel(dg, dg_ref) < 1e-13
+        assert np.array_equal(piv, ob.topk(dg, k))          # same rule on the same diagonal: exact
+        pc = ob.PartialCholesky(rp, ci, v, d, lp.m, lp.n, k, ob.PIVOT_GIVEN, piv)
+        non = np.ones(lp.m, bool)
+        non[piv] = False
+        ds_ref = pc.diag_s
+        good = non & (ds_ref > 1e-6 * dg_ref)              # rows whose Schur diagonal is not pure cancellation
+        assert np.max(np.abs(ds[good] - ds_ref[good]) / dg_ref[good]) < 1e-9
+        r = rng.standard_normal(lp.m)
+        z = g.precond_apply(r)
+        assert rel(z, pc.apply(r)) < 1e-8
+
+
+def test_cg_matches_oracle(case):
+    name, lp, d, rng = case
+    rp, ci, v = lp.csr()
+    k = 16
+    b = rng.standard_normal(lp.m)
+    with backend.GpuNormalEquations(pivots=k, cg_tol=1e-10, cg_max_iter=20000) as g:
+        g.LinearEquation_Construct(lp)
+        g.RenewLinearEquation(d)
+        piv, _, _ = g.pivots()
+        x, it = g.cg(b)
+    xo, ito = ob.pcg(rp, ci, v, d, b, lp.m, lp.n, k, ob.PIVOT_GIVEN, piv, tol=1e-10, max_iter=20000)
+    assert rel(x, xo) < 1e-6
+    assert abs(it - ito) <= max(3, 0.05 * ito)
+
+
+def test_solve_linear_equation(case):
+    name, lp, d, rng = case
+    b1 = rng.standard_normal(lp.n)
+    b2 = rng.standard_normal(lp.m)
+    with backend.GpuNormalEquations(pivots=10, cg_tol=1e-12, cg_max_iter=50000) as g:
+        g.LinearEquation_Construct(lp)
+        g.RenewLinearEquation(d)
+        x1, x2 = g.SolveLinearEquation(d, b1, b2)
+        st = g.stats()
+    ora = ob.OracleNormalEquations(pivots=10, rule=ob.PIVOT_GIVEN, tol=1e-12, max_iter=50000)
+    ora.LinearEquation_Construct(lp)
+    ox1, ox2 = ora.SolveLinearEquation(d, b1, b2)
+    assert st["converged"] == 1
+    assert rel(x2, ox2) < 1e-6
+    assert rel(x1, ox1) < 1e-6
+
+
+def test_mixed_precision_solve(case):
+    name, lp, d, rng = case
+    b1 = rng.standard_normal(lp.n)
+    b2 = rng.standard_normal(lp.m)
+    with backend.GpuNormalEquations(pivots=16, precision="mixed", ir_tol=1e-10, inner_tol=1e-4,
+                                    cg_tol=1e-14) as g:
+        g.LinearEquation_Construct(lp)
+        g.RenewLinearEquation(d)
+        x1, x2 = g.SolveLinearEquation(d, b1, b2)
+        st = g.stats()
+    ora = ob.OracleNormalEquations(pivots=16, rule=ob.PIVOT_GIVEN, tol=1e-14, max_iter=100000)
+    ora.LinearEquation_Construct(lp)
+    ox1, ox2 = ora.SolveLinearEquation(d, b1, b2)
+    assert st["rel_residual"] < 1e-9
+    assert rel(x2, ox2) < 1e-5
+
+
+def test_adat_assembly_bitwise(case):
+    name, lp, d, rng = case
+    rp, ci, v = lp.csr()
+    if name == "zipf":
+        pytest.skip("rows beyond the explicit assembly's per-row capacity")
+    w = np.exp(rng.uniform(-2, 2, lp.n))
+    with backend.GpuNormalEquations(pivots=1) as g:
+        g.LinearEquation_Construct(lp)
+        grp, gcol, gval = g.adat(w)
+    import ctypes as C
+    orp = np.zeros(lp.m + 1, np.int32)
+    nnz = ob.lib().oracle_adat_symbolic(lp.m, lp.n, ob.P(rp), ob.P(ci), ob.P(lp.col_ptr), ob.P(lp.row_ind),
+                                        ob.P(orp), None)
+    ocol = np.zeros(nnz, np.int32)
+    ob.lib().oracle_adat_symbolic(lp.m, lp.n, ob.P(rp), ob.P(ci), ob.P(lp.col_ptr), ob.P(lp.row_ind), ob.P(orp),
+                                  ob.P(ocol))
+    oval = np.zeros(nnz)
+    ob.lib().oracle_adat_numeric(lp.m, lp.n, ob.P(rp), ob.P(ci), ob.P(v), ob.P(lp.col_ptr), ob.P(lp.row_ind),
+                                 ob.P(lp.val), ob.P(w), ob.P(orp), ob.P(ocol), ob.P(oval))
+    assert np.array_equal(grp, orp)
+    for i in range(lp.m):
+        a, b = orp[i], orp[i + 1]
+        o = np.argsort(ocol[a:b], kind="stable")
+        assert np.array_equal(gcol[a:b], ocol[a:b][o])
+        assert np.array_equal(gval[a:b], oval[a:b][o])   # same products, same order: bit-exact
+
+
+def test_bad_d_is_an_error():
+    lp = CASES["random"]()
+    with backend.GpuNormalEquations(pivots=4) as g:
+        g.LinearEquation_Construct(lp)
+        d = np.ones(lp.n)
+        d[7] = 0.0
+        with pytest.raises(backend.BackendError) as e:
+            g.RenewLinearEquation(d)
+        assert e.value.code == -4
+        d[7] = np.nan
+        with pytest.raises(backend.BackendError):
+            g.RenewLinearEquation(d)
+        g.RenewLinearEquation(np.ones(lp.n))          # context still usable afterwards
+        assert g.stats()["pivots"] == 4

@@ -1,0 +1,113 @@
+"""Host-side pieces: generator determinism and feasibility, MPS round trip,
+C-ABI symbol exports (no GPU compute), HSD driver on small LPs vs scipy."""
+import ctypes as C
+import hashlib
+import os
+import re
+import tempfile
+
+import numpy as np
+import pytest
+
+from help_gb300 import hsd, lp as L, native
+from oracle import bindings as ob
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _digest(lp):
+    h = hashlib.sha256()
+    for a in (lp.col_ptr, lp.row_ind, lp.val, lp.b, lp.c):
+        h.update(np.ascontiguousarray(a).tobytes())
+    return h.hexdigest()[:16]
+
+
+def test_generator_deterministic():
+    a = L.generate(L.spec_random(300, 900, 5), 42)
+    b = L.generate(L.spec_random(300, 900, 5), 42)
+    c = L.generate(L.spec_random(300, 900, 5), 43)
+    assert _digest(a) == _digest(b)
+    assert _digest(a) != _digest(c)
+
+
+@pytest.mark.parametrize("spec", [
+    L.spec_random(500, 1500, 5),
+    L.spec_zipf(2000, 8000, 6),
+    L.spec_block(3, 200, 900, 5, 30, 0.05),
+])
+def test_generator_feasible_by_construction(spec):
+    lp = L.generate(spec, 9)
+    assert lp.col_ptr[0] == 0 and np.all(np.diff(lp.col_ptr) >= 0)
+    for j in range(lp.n):
+        r = lp.row_ind[lp.col_ptr[j]:lp.col_ptr[j + 1]]
+        assert np.all(np.diff(r) > 0)
+    rows_hit = np.bincount(lp.row_ind, minlength=lp.m)
+    assert rows_hit.min() >= 1, "empty row"
+    assert np.all(lp.val != 0)
+    # values on the 1e-6 grid
+    assert np.all(np.abs(lp.val * 1e6 - np.round(lp.val * 1e6)) < 1e-6)
+
+
+def test_zipf_rows_are_skewed():
+    lp = L.generate(L.spec_zipf(20000, 80000, 6), 1)
+    cnt = np.bincount(lp.row_ind, minlength=lp.m)
+    assert cnt.max() > 20 * cnt.mean()
+
+
+def test_mcf_shape():
+    lp = L.generate(L.spec_mcf(10, 2, 3), 1)
+    arcs = 4 * 10 * 9
+    assert lp.n == 2 * arcs + arcs and lp.n_struct == 2 * arcs
+    assert lp.m == 2 * (100 - 1) + arcs
+    assert lp.row_type.count(b"L") == arcs
+
+
+def test_mps_round_trip():
+    lp = L.generate(L.spec_random(30, 90, 4), 5)
+    with tempfile.TemporaryDirectory() as t:
+        p = os.path.join(t, "a.mps")
+        lp.write_mps(p)
+        txt = open(p).read().splitlines()
+    # fixed card positions 4 / 14 / 24, each line short enough not to carry a second pair
+    cols = [l for l in txt if l.startswith("    C")]
+    assert all(len(l) <= 39 for l in cols)
+    vals = {}
+    for l in cols:
+        name, row, v = l[4:12].strip(), l[14:22].strip(), float(l[24:])
+        if row != "COST":
+            vals[(int(row[1:]), int(name[1:]))] = v
+    for j in range(lp.n):
+        for p_ in range(lp.col_ptr[j], lp.col_ptr[j + 1]):
+            assert vals[(lp.row_ind[p_], j)] == lp.val[p_]
+
+
+def _declared(header):
+    txt = open(os.path.join(ROOT, "include", header)).read()
+    return sorted(set(re.findall(r"\b(help_[a-z0-9_]+)\s*\(", txt)))
+
+
+def test_gpu_library_exports_every_declared_symbol():
+    path = os.path.join(native.LIBDIR, "libhelp_gpu.so")
+    lib = C.CDLL(path)  # loads without a GPU (no compute)
+    names = _declared("help_gpu.h")
+    assert len(names) >= 14
+    for s in names:
+        getattr(lib, s)
+
+
+def test_lp_library_exports_every_declared_symbol():
+    lib = C.CDLL(os.path.join(native.LIBDIR, "libhelp_lp.so"))
+    for s in _declared("help_lp.h"):
+        getattr(lib, s)
+
+
+def test_hsd_driver_objective_matches_scipy():
+    scipy_opt = pytest.importorskip("scipy.optimize")
+    import scipy.sparse as sp
+    lp = L.generate(L.spec_random(80, 240, 5), 3)
+    ora = ob.OracleNormalEquations(pivots=10, tol=1e-14, max_iter=10**6)
+    res = hsd.solve_lp(lp, ora.ne_backend())
+    A = sp.csc_matrix((lp.val, lp.row_ind, lp.col_ptr), shape=(lp.m, lp.n))
+    r = scipy_opt.linprog(lp.c, A_eq=A, b_eq=lp.b, bounds=(0, None), method="highs")
+    assert res["status"] == 0
+    assert abs(res["primal_obj"] - r.fun) / (1 + abs(r.fun)) < 1e-8
