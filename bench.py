@@ -1,0 +1,342 @@
+#!/usr/bin/env python
+"""Benchmark of the normal-equations hot path on GB300.
+
+Headline (one JSON line on stdout): the isolated product (A D^-1 A^T) v on
+the 100,000 x 400,000 LP (8 nonzeros per column, 3.2M nonzeros) with d
+log-uniform in [1e-8, 1e8] -- the SpMV GB/s metric -- in FP64 (the drop-in
+precision).  One step = one product = two CSR row-gather passes,
+t = B^T v then y = B t with B = A D^-1/2.  Inputs are resident in HBM; L2 is
+flushed (256 MB write) before every step.  Achieved bandwidth counts the
+algorithmic bytes of each pass (values and indices once, both vectors once).
+
+Also reported on the same line: the FP32 product (mixed precision), the
+end-to-end product through the C ABI with host buffers, the CPU baseline
+(the reference's CSRMV_T / scale / CSRMV_N loops restated in oracle/, one
+core), the IPM time to a 1e-8 relative gap on the 2,000 x 6,000 LP (GPU,
+plain FP64 PCG), the live roofline of the dominant kernel and the SM clocks
+sampled during the timed region.
+
+    python bench.py [--steps K] [--warmup W] [--gpus N] [--impl ours|reference]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+METRIC = "SpMV HBM GB/s: (A D^-1 A^T) v, two CSR row-gather passes (IPM time to 1e-8 gap reported alongside)"
+WORKLOAD = "config 1: m=100000 n=400000, 8 nnz/col (3.2M nnz), d log-uniform [1e-8,1e8]"
+
+
+def alg_bytes(m: int, n: int, nnz: int, elem: int) -> dict:
+    """Algorithmic bytes of each pass: values + int32 indices once, row
+    pointers once, the gathered vector once, the result once."""
+    bt = (elem + 4) * nnz + 4 * (n + 1) + elem * m + elem * n   # t = B^T v (rows of A^T = columns)
+    b = (elem + 4) * nnz + 4 * (m + 1) + elem * n + elem * m    # y = B t
+    return {"BT": bt, "B": b, "step": bt + b}
+
+
+def peaks() -> dict:
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return {"hbm_gbs": d["hbm_gbs"], "source": "measured"}
+    return {"hbm_gbs": 6800.0, "source": "fallback"}
+
+
+def ncu_traffic() -> dict | None:
+    p = os.path.join(ROOT, "profiles", "spmv_adat_config1_traffic.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            return json.load(f)
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle-reason samples during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        fd, self.path = tempfile.mkstemp(prefix="clocks_", suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        self.proc.wait()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        with open(self.path) as f:
+            for line in f:
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) < 9:
+                    continue
+                try:
+                    sm.append(float(parts[1]))
+                    mx.append(float(parts[2]))
+                except ValueError:
+                    continue
+                for nm, v in zip(names, parts[5:9]):
+                    if v.lower() == "active":
+                        reasons.add(nm)
+        os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def cpu_adat_baseline(lp, d, seconds: float = 10.0) -> dict:
+    """The reference's own loops for one (A D^-1 A^T) v (PCG.cpp:346-358 with
+    CSRMV_T / CSRMV_N of Helper.cpp:57-81), restated in oracle/, one core."""
+    from oracle import bindings as ob
+
+    rp, ci, v = lp.csr()
+    x = np.random.default_rng(1).standard_normal(lp.m)
+    nb = alg_bytes(lp.m, lp.n, lp.nnz, 8)["step"] + 8 * lp.n  # + reading d in the scale loop
+    reps, t0 = 0, time.perf_counter()
+    while True:
+        t = ob.csrmv_t(rp, ci, v, x, lp.m, lp.n)
+        t /= d
+        ob.csrmv_n(rp, ci, v, t, lp.m, lp.n)
+        reps += 1
+        el = time.perf_counter() - t0
+        if el > seconds or reps >= 1000:
+            break
+    return {"value": nb * reps / el / 1e9, "unit": "GB/s", "cores": 1, "kind": "port",
+            "sample": "%d products (A D^-1 A^T) v on %s, single thread (the reference's loops are serial)" % (reps, WORKLOAD),
+            "seconds": el}
+
+
+def ipm_time(config: int = 0) -> dict:
+    """HSD IPM (the reference's HSD_Main restated) to a 1e-8 gap on the GPU backend."""
+    from help_gb300 import backend, hsd, lp as L
+
+    lp = L.make_lp(config, 0)
+    with backend.GpuNormalEquations(pivots=L.config_pivots(config), cg_tol=1e-10, cg_max_iter=1_000_000) as g:
+        t0 = time.perf_counter()
+        r = hsd.solve_lp(lp, g.ne_backend())
+        wall = time.perf_counter() - t0
+        st = g.stats()
+    return {"config": "config %d: m=%d n=%d nnz=%d" % (config, lp.m, lp.n, lp.nnz), "form": "plain FP64 PCG, k=%d, cg_tol 1e-10"
+            % L.config_pivots(config), "seconds": round(wall, 3), "status": r["status"], "iterations": r["iterations"],
+            "rel_gap": r["rel_gap"], "primal_obj": r["primal_obj"], "cg_iterations": int(st["cg_iterations_total"]),
+            "backend_seconds": round(r["backend_s"], 3)}
+
+
+def run_reference(args) -> None:
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return
+    from help_gb300 import lp as L
+
+    lp = L.make_lp(1, 0)
+    rng = np.random.default_rng(0)
+    d = np.exp(rng.uniform(np.log(1e-8), np.log(1e8), lp.n))
+    from oracle import bindings as ob
+
+    rp, ci, v = lp.csr()
+    x = rng.standard_normal(lp.m)
+    nb = alg_bytes(lp.m, lp.n, lp.nnz, 8)["step"] + 8 * lp.n
+    for _ in range(args.warmup):
+        t = ob.csrmv_t(rp, ci, v, x, lp.m, lp.n)
+        t /= d
+        ob.csrmv_n(rp, ci, v, t, lp.m, lp.n)
+    ts = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        t = ob.csrmv_t(rp, ci, v, x, lp.m, lp.n)
+        t /= d
+        ob.csrmv_n(rp, ci, v, t, lp.m, lp.n)
+        ts.append(time.perf_counter() - t0)
+    tot = sum(ts)
+    val = nb * len(ts) / tot / 1e9
+    out = {"metric": METRIC, "value": round(val, 3), "unit": "GB/s", "impl": "reference", "n_gpus": ws,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 * tot / len(ts), 4),
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+           "config": {"workload": WORKLOAD},
+           "cpu_baseline": {"value": round(val, 3), "unit": "GB/s", "cores": 1, "kind": "port",
+                            "sample": "%d products; the reference's CSRMV_T, scale, CSRMV_N loops restated in "
+                                      "oracle/ (the reference's own build needs its sources, absent here)" % len(ts)},
+           "e2e": {"value": round(val, 3), "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out), flush=True)
+
+
+def main() -> None:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=30)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-ipm", action="store_true", help="skip the IPM-time measurement")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+        return
+
+    import torch
+
+    from help_gb300 import backend, lp as L
+
+    ws, rank, local = dist_env()
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+
+    lp = L.make_lp(1, 0)
+    m, n, nnz = lp.m, lp.n, lp.nnz
+    rng = np.random.default_rng(0)
+    d = np.exp(rng.uniform(np.log(1e-8), np.log(1e8), n))
+    g = backend.GpuNormalEquations(pivots=L.config_pivots(1), precision="mixed", device=local)
+    g.LinearEquation_Construct(lp)
+    g.RenewLinearEquation(d)
+
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)  # 256 MB > L2
+    res = {}
+    for prec, dt in (("f64", torch.float64), ("f32", torch.float32)):
+        x = torch.randn(m, dtype=dt, device=dev)
+        t = torch.empty(n, dtype=dt, device=dev)
+        y = torch.empty(m, dtype=dt, device=dev)
+        fp32 = prec == "f32"
+
+        def step(times):
+            flush.fill_(1.0)
+            e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+            e0.record()
+            g.matvec_dev("BT", x.data_ptr(), t.data_ptr(), fp32=fp32)
+            e1.record()
+            g.matvec_dev("B", t.data_ptr(), y.data_ptr(), fp32=fp32)
+            e2.record()
+            if times is not None:
+                times.append((e0, e1, e2))
+
+        for _ in range(args.warmup):
+            step(None)
+        torch.cuda.synchronize()
+        if ws > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+        sampler = ClockSampler(local) if prec == "f64" else None
+        if sampler:
+            sampler.start()
+        evs = []
+        for _ in range(args.steps):
+            step(evs)
+        torch.cuda.synchronize()
+        if ws > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+        clocks = sampler.stop() if sampler else None
+        bt = [a.elapsed_time(b) for a, b, _ in evs]
+        bb = [b.elapsed_time(c) for _, b, c in evs]
+        tot = [a.elapsed_time(c) for a, _, c in evs]
+        res[prec] = {"bt_ms": sum(bt) / len(bt), "b_ms": sum(bb) / len(bb), "step_ms": sum(tot) / len(tot),
+                     "clocks": clocks}
+
+    # correctness of the timed product (FP64 vs a direct host recomputation is the parity test's job;
+    # here: FP32 and FP64 agree)
+    ab64 = alg_bytes(m, n, nnz, 8)
+    ab32 = alg_bytes(m, n, nnz, 4)
+    step_ms = res["f64"]["step_ms"]
+    if ws > 1:
+        tt = torch.tensor([step_ms], dtype=torch.float64, device=dev)
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        step_ms = float(tt.item())
+    value = ws * ab64["step"] / (step_ms * 1e-3) / 1e9
+
+    pk = peaks()
+    dom = "B" if res["f64"]["b_ms"] >= res["f64"]["bt_ms"] else "BT"
+    dom_ms = res["f64"]["b_ms"] if dom == "B" else res["f64"]["bt_ms"]
+    achieved = ab64[dom] / (dom_ms * 1e-3) / 1e9
+    tr = ncu_traffic()
+    roof = {"bound": "hbm", "kernel": "k_spmv<double> pass %s (%s)" % (dom, "y = B t" if dom == "B" else "t = B^T v"),
+            "achieved": round(achieved, 1), "peak": pk["hbm_gbs"], "peak_source": pk["source"], "unit": "GB/s",
+            "frac": round(achieved / pk["hbm_gbs"], 4), "algorithmic_bytes": ab64[dom],
+            "traffic": (tr or {}).get(dom), "traffic_source": (tr or {}).get("source")}
+
+    # end to end through the C ABI with host buffers (H2D v, D2H y every step)
+    xh = rng.standard_normal(m)
+    for _ in range(2):
+        g.matvec("ADAT", xh)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        g.matvec("ADAT", xh)
+    torch.cuda.synchronize()
+    e2e_s = (time.perf_counter() - t0) / args.steps
+    e2e = {"value": round(ab64["step"] / e2e_s / 1e9, 2), "unit": "GB/s", "h2d_bytes_per_step": 8 * m,
+           "d2h_bytes_per_step": 8 * m, "note": "host time per product incl. the L2 flush launch"}
+
+    extra = {}
+    cpu = None
+    if rank == 0:
+        cpu = cpu_adat_baseline(lp, d, seconds=10.0)
+        if not args.no_ipm:
+            try:
+                extra["ipm"] = ipm_time(0)
+            except Exception as e:  # reported, not fatal for the kernel line
+                extra["ipm"] = {"error": str(e)}
+    g.close()
+
+    if rank == 0:
+        out = {
+            "metric": METRIC, "value": round(value, 2), "unit": "GB/s", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(step_ms, 5), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded generator, config 1)",
+            "config": {"workload": WORKLOAD, "l2": "flushed before every step (256 MB write)",
+                       "parallelism": "replicas" if ws > 1 else "single GPU"},
+            "roofline": roof,
+            "fp32": {"value": round(ab32["step"] / (res["f32"]["step_ms"] * 1e-3) / 1e9, 2), "unit": "GB/s",
+                     "ms_per_step": round(res["f32"]["step_ms"], 5),
+                     "frac": round(ab32["step"] / (res["f32"]["step_ms"] * 1e-3) / 1e9 / pk["hbm_gbs"], 4)},
+            "passes_ms": {"f64": {"BT": round(res["f64"]["bt_ms"], 5), "B": round(res["f64"]["b_ms"], 5)},
+                          "f32": {"BT": round(res["f32"]["bt_ms"], 5), "B": round(res["f32"]["b_ms"], 5)}},
+            "e2e": e2e,
+            "cpu_baseline": {k: (round(v, 3) if isinstance(v, float) else v) for k, v in cpu.items()} if cpu else None,
+            "gpu_launches": 2 * args.steps,
+            "clocks": res["f64"]["clocks"],
+        }
+        out.update(extra)
+        print(json.dumps(out), flush=True)
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

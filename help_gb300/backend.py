@@ -135,16 +135,18 @@ class GpuNormalEquations:
         return {f: getattr(s, f) for f, _ in native.PcgStats._fields_}
 
     def matvec(self, op: str, x) -> np.ndarray:
-        opc = {"A": native.HELP_OP_A, "AT": native.HELP_OP_AT, "ADAT": native.HELP_OP_ADAT}[op]
-        nin = self.n if op == "A" else self.m
-        nout = self.n if op == "AT" else self.m
+        opc = {"A": native.HELP_OP_A, "AT": native.HELP_OP_AT, "ADAT": native.HELP_OP_ADAT,
+               "B": native.HELP_OP_B, "BT": native.HELP_OP_BT}[op]
+        nin = self.n if op in ("A", "B") else self.m
+        nout = self.n if op in ("AT", "BT") else self.m
         x = _f64(x, nin)
         y = np.empty(nout)
         self._check(self.lib.help_pcg_matvec(self.ctx, opc, native.ptr(x), native.ptr(y)))
         return y
 
     def matvec_dev(self, op: str, x_ptr: int, y_ptr: int, fp32: bool = False, stream: int = 0) -> None:
-        opc = {"A": native.HELP_OP_A, "AT": native.HELP_OP_AT, "ADAT": native.HELP_OP_ADAT}[op]
+        opc = {"A": native.HELP_OP_A, "AT": native.HELP_OP_AT, "ADAT": native.HELP_OP_ADAT,
+               "B": native.HELP_OP_B, "BT": native.HELP_OP_BT}[op]
         self._check(self.lib.help_pcg_matvec_dev(self.ctx, opc, int(fp32), C.c_void_p(x_ptr),
                                                  C.c_void_p(y_ptr), C.c_void_p(stream or None)))
 

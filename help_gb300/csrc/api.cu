@@ -7,6 +7,8 @@
 #include <algorithm>
 #include <chrono>
 #include <cmath>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <new>
 #include <string>
@@ -44,15 +46,46 @@ double now_ms() {
 
 DevCtrl* ctrl_of(help_pcg* ctx) { return ctx->ctrl.as<DevCtrl>(); }
 
-int upload_items(help_pcg* ctx, ItemList& L, const int32_t* ptr, int32_t rows, int cap) {
-    std::vector<Int4> v = plan_items(ptr, rows, cap, 512, 48);
-    L.n = (int32_t)v.size();
-    L.cap = cap;
-    CK(L.buf.ensure(sizeof(Int4) * std::max<size_t>(v.size(), 1)));
-    if (!v.empty()) CK(cudaMemcpyAsync(L.buf.p, v.data(), sizeof(Int4) * v.size(), cudaMemcpyHostToDevice, ctx->stream));
-    CK(cudaStreamSynchronize(ctx->stream));  // v goes out of scope
+int upload_split(help_pcg* ctx, RowSplit& S, const int32_t* ptr, int32_t rows, int g_min) {
+    RowPlanHost h = plan_rows(ptr, rows, g_min);
+    S.G = h.G;
+    S.short_max = h.short_max;
+    S.n_med = (int32_t)h.med.size();
+    S.n_long = (int32_t)h.lng.size();
+    CK(S.med.ensure(4 * std::max<size_t>(h.med.size(), 1)));
+    CK(S.lng.ensure(4 * std::max<size_t>(h.lng.size(), 1)));
+    if (!h.med.empty()) CK(cudaMemcpyAsync(S.med.p, h.med.data(), 4 * h.med.size(), cudaMemcpyHostToDevice, ctx->stream));
+    if (!h.lng.empty()) CK(cudaMemcpyAsync(S.lng.p, h.lng.data(), 4 * h.lng.size(), cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));  // h goes out of scope
     return HELP_OK;
 }
+
+int upload_plan(help_pcg* ctx, RowPlan& P, const int32_t* ptr, int32_t rows, bool with_f32) {
+    P.rows = rows;
+    int rc = upload_split(ctx, P.s64, ptr, rows, kGminF64);
+    if (!rc && with_f32) rc = upload_split(ctx, P.s32, ptr, rows, kGminF32);
+    return rc;
+}
+
+template <class V>
+SpmvView<V> view(const RowPlan& P, const DevMem& ptr, const DevMem& idx, const DevMem& val) {
+    const RowSplit& S = std::is_same<V, float>::value ? P.s32 : P.s64;
+    SpmvView<V> v;
+    v.rows = P.rows;
+    v.G = S.G;
+    v.short_max = S.short_max;
+    v.n_med = S.n_med;
+    v.n_long = S.n_long;
+    v.ptr = ptr.as<int>();
+    v.idx = idx.as<int>();
+    v.val = val.as<V>();
+    v.med_rows = S.med.as<int>();
+    v.long_rows = S.lng.as<int>();
+    return v;
+}
+
+int spmv_blocks(help_pcg* ctx) { return ctx->num_sms * 8; }
+constexpr int kSpmvThreads = 256;
 
 int ensure_stage(help_pcg* ctx, size_t elems) {
     if (ctx->h_stage_elems >= elems) return HELP_OK;
@@ -107,42 +140,22 @@ struct CgResult {
 template <class V>
 int run_pcg(help_pcg* ctx, V* x, V* r0, double tol, long long max_iter, int precond_only, CgResult* res) {
     const bool f32 = std::is_same<V, float>::value;
-    PcgArgs<V> A{};
+    const int slot = f32 ? 1 : 0;
+    const int nb = ctx->cg_blocks;
+    CgArgs<V> A;
+    std::memset(&A, 0, sizeof(A));
     A.m = ctx->m;
     A.n = ctx->n;
     A.k = ctx->k;
-    const ItemList& icsr = f32 ? ctx->it_csr32 : ctx->it_csr;
-    const ItemList& icsc = f32 ? ctx->it_csc32 : ctx->it_csc;
-    const ItemList& ic = f32 ? ctx->it_c32 : ctx->it_c;
-    const ItemList& ict = f32 ? ctx->it_ct32 : ctx->it_ct;
-    A.cap = icsr.cap;
-    A.csr_items = icsr.items();
-    A.n_csr = icsr.n;
-    A.rp = ctx->rp.as<int>();
-    A.ci = ctx->ci.as<int>();
-    A.bv = f32 ? (const V*)ctx->bv32.p : (const V*)ctx->bv.p;
-    A.csc_items = icsc.items();
-    A.n_csc = icsc.n;
-    A.cp = ctx->cp.as<int>();
-    A.ri = ctx->ri.as<int>();
-    A.bvT = f32 ? (const V*)ctx->bvT32.p : (const V*)ctx->bvT.p;
-    A.c_items = ic.items();
-    A.n_c = ic.n;
-    A.c_rp = ctx->c_rp.as<int>();
-    A.c_ci = ctx->c_ci.as<int>();
-    A.c_v = f32 ? (const V*)ctx->c_v32.p : (const V*)ctx->c_v.p;
-    A.ct_items = ict.items();
-    A.n_ct = ict.n;
-    A.ct_rp = ctx->ct_rp.as<int>();
-    A.ct_ci = ctx->ct_ci.as<int>();
-    A.ct_v = f32 ? (const V*)ctx->ct_v32.p : (const V*)ctx->ct_v.p;
+    A.csr = view<V>(ctx->pl_csr, ctx->rp, ctx->ci, f32 ? ctx->bv32 : ctx->bv);
+    A.csc = view<V>(ctx->pl_csc, ctx->cp, ctx->ri, f32 ? ctx->bvT32 : ctx->bvT);
+    A.c = view<V>(ctx->pl_c, ctx->c_rp, ctx->c_ci, f32 ? ctx->c_v32 : ctx->c_v);
+    A.ct = view<V>(ctx->pl_ct, ctx->ct_rp, ctx->ct_ci, f32 ? ctx->ct_v32 : ctx->ct_v);
     A.piv = ctx->piv.as<int>();
     A.pivpos = ctx->pivpos.as<int>();
     A.W = ctx->W.as<double>();
     A.dsinv = f32 ? (const V*)ctx->dsinv32.p : (const V*)ctx->dsinv.p;
     A.delta = ctx->opt.delta;
-    A.tol2 = tol * tol;
-    A.max_iter = max_iter;
     A.x = x;
     A.r0 = r0;
     A.r1 = f32 ? (V*)ctx->r132.p : (V*)ctx->r1.p;
@@ -153,40 +166,69 @@ int run_pcg(help_pcg* ctx, V* x, V* r0, double tol, long long max_iter, int prec
     A.t = f32 ? (V*)ctx->t32.p : (V*)ctx->t.p;
     A.a = ctx->a.as<double>();
     A.w = ctx->w.as<double>();
-    A.part = ctx->partials.as<double>();
+    double* part = ctx->cg_part.as<double>();
+    A.part_rr = part;
+    A.part_rz = part + nb;
+    A.part_aw = part + 2 * nb;
+    A.part_pq = part + 3 * nb;
     A.precond_only = precond_only;
     DevCtrl* c = ctrl_of(ctx);
-    A.bar.count = &c->bar_count;
-    A.bar.gen = &c->bar_gen;
-    A.bar.status = &c->status;
-    A.out = &c->cg;
-    const int blocks = f32 ? ctx->coop_blocks_f32 : ctx->coop_blocks_f64;
-    const size_t smem = std::max(spmv_smem_bytes<V>(A.cap), (size_t)std::max(ctx->k, 1) * sizeof(double));
-    if ((size_t)blocks * 3 > (size_t)kPartElems) return fail(ctx, HELP_E_ARG, "too many persistent blocks");
-    CK(cudaMemsetAsync(c, 0, 2 * sizeof(unsigned int), ctx->stream));
-    CK(pcg_launch<V>(A, blocks, ctx->threads, smem, ctx->stream));
-    CgOutDev out{};
-    CK(cudaMemcpyAsync(&out, &c->cg, sizeof(out), cudaMemcpyDeviceToHost, ctx->stream));
-    CK(cudaStreamSynchronize(ctx->stream));
-    int rc = read_status(ctx, "pcg");
-    if (rc) return rc;
-    res->iterations = out.iterations;
-    res->rr0 = out.rr0;
-    res->rr = out.rr;
-    res->converged = out.converged;
-    res->status = out.status;
-    if (out.status != 0) return fail(ctx, HELP_E_NUMERIC, "pcg: breakdown (non-positive curvature or NaN)");
+    A.sc = &c->cg;
+    // scalars the host sets: tolerance and cap (everything else the init kernel writes)
+    CgScalars* h = ctx->h_sc;
+    std::memset(h, 0, sizeof(*h));
+    h->tol2 = tol * tol;
+    h->max_iter = max_iter;
+    CK(cudaMemcpyAsync(&c->cg, h, sizeof(CgScalars), cudaMemcpyHostToDevice, ctx->stream));
+    // (re)capture the per-iteration graph when the arguments changed
+    std::vector<unsigned char>& key = ctx->graph_args[slot];
+    if (!ctx->graph_exec[slot] || key.size() != sizeof(A) || std::memcmp(key.data(), &A, sizeof(A)) != 0) {
+        if (ctx->graph_exec[slot]) {
+            cudaGraphExecDestroy(ctx->graph_exec[slot]);
+            ctx->graph_exec[slot] = nullptr;
+        }
+        cudaGraph_t g = nullptr;
+        CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+        cudaError_t ce = cudaSuccess;
+        for (int u = 0; u < kGraphIters && ce == cudaSuccess; ++u) ce = cg_launch_iteration<V>(A, nb, ctx->stream);
+        cudaError_t ee = cudaStreamEndCapture(ctx->stream, &g);
+        CK(ce);
+        CK(ee);
+        ee = cudaGraphInstantiate(&ctx->graph_exec[slot], g, 0);
+        cudaGraphDestroy(g);
+        CK(ee);
+        key.assign((const unsigned char*)&A, (const unsigned char*)&A + sizeof(A));
+    }
+    CK(cudaEventRecord(ctx->ev0, ctx->stream));
+    CK(cg_launch_init<V>(A, nb, ctx->stream));
+    for (;;) {
+        CK(cudaGraphLaunch(ctx->graph_exec[slot], ctx->stream));
+        CK(cudaMemcpyAsync(h, &c->cg, sizeof(CgScalars), cudaMemcpyDeviceToHost, ctx->stream));
+        CK(cudaStreamSynchronize(ctx->stream));
+        if (h->done != 0 || precond_only) break;
+    }
+    CK(cudaEventRecord(ctx->ev1, ctx->stream));
+    CK(cudaEventSynchronize(ctx->ev1));
+    float kms = 0.f;
+    CK(cudaEventElapsedTime(&kms, ctx->ev0, ctx->ev1));
+    ctx->solve_kernel_ms += kms;
+    ctx->solve_launches += 1;
+    if (f32) ctx->solve_iters_f32 += h->it;
+    res->iterations = h->it;
+    res->rr0 = h->rr0;
+    res->rr = h->rr;
+    res->converged = (h->done == 1);
+    res->status = h->status;
+    if (h->done == 3) return fail(ctx, HELP_E_NUMERIC, "pcg: breakdown (non-positive curvature or NaN)");
     return HELP_OK;
 }
 
 // res = rhs - G x  (FP64), returns ||res||^2 in *rr (host)
 int residual_f64(help_pcg* ctx, const double* x, const double* rhs, double* res, double* rr) {
-    CK(spmv_launch<double>(kEpiStore, ctx->it_csc.items(), ctx->it_csc.n, ctx->cp.as<int>(), ctx->ri.as<int>(),
-                           ctx->bvT.as<double>(), ctx->it_csc.cap, x, ctx->t.as<double>(), nullptr, nullptr, nullptr,
-                           0.0, 0, ctx->threads, ctx->stream));
-    CK(spmv_launch<double>(kEpiResid, ctx->it_csr.items(), ctx->it_csr.n, ctx->rp.as<int>(), ctx->ci.as<int>(),
-                           ctx->bv.as<double>(), ctx->it_csr.cap, ctx->t.as<double>(), res, rhs, x, nullptr,
-                           ctx->opt.delta, 0, ctx->threads, ctx->stream));
+    CK(spmv_launch<double>(kEpiStore, view<double>(ctx->pl_csc, ctx->cp, ctx->ri, ctx->bvT), x, ctx->t.as<double>(),
+                           nullptr, nullptr, nullptr, 0.0, spmv_blocks(ctx), kSpmvThreads, ctx->stream));
+    CK(spmv_launch<double>(kEpiResid, view<double>(ctx->pl_csr, ctx->rp, ctx->ci, ctx->bv), ctx->t.as<double>(), res,
+                           rhs, x, nullptr, ctx->opt.delta, spmv_blocks(ctx), kSpmvThreads, ctx->stream));
     if (rr) {
         double* part = ctx->partials.as<double>() + 4096;
         CK(vec_sumsq(res, ctx->m, part, part + 2048, ctx->stream));
@@ -335,11 +377,20 @@ void release_all(help_pcg* ctx) {
                       &ctx->rhs,    &ctx->b1,    &ctx->b2,     &ctx->x1,     &ctx->x2,    &ctx->res,   &ctx->xacc,
                       &ctx->adat_tmp};
     for (DevMem* b : bufs) b->release();
-    ItemList* lists[] = {&ctx->it_csr, &ctx->it_csc, &ctx->it_csr32, &ctx->it_csc32,
-                         &ctx->it_c,   &ctx->it_ct,  &ctx->it_c32,   &ctx->it_ct32};
-    for (ItemList* l : lists) {
-        l->buf.release();
-        l->n = 0;
+    ctx->cg_part.release();
+    for (int s = 0; s < 2; ++s) {
+        if (ctx->graph_exec[s]) cudaGraphExecDestroy(ctx->graph_exec[s]);
+        ctx->graph_exec[s] = nullptr;
+        ctx->graph_args[s].clear();
+    }
+    RowPlan* plans[] = {&ctx->pl_csr, &ctx->pl_csc, &ctx->pl_c, &ctx->pl_ct};
+    for (RowPlan* p : plans) {
+        for (RowSplit* s : {&p->s64, &p->s32}) {
+            s->med.release();
+            s->lng.release();
+            s->n_med = s->n_long = 0;
+        }
+        p->rows = 0;
     }
 }
 
@@ -434,23 +485,15 @@ int renew_impl(help_pcg* ctx, const double* d_host) {
     ctx->h_tmp.resize((size_t)m + 1);
     CK(cudaMemcpyAsync(ctx->h_tmp.data(), ctx->c_rp.p, 4 * ((size_t)m + 1), cudaMemcpyDeviceToHost, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
-    rc = upload_items(ctx, ctx->it_c, ctx->h_tmp.data(), m, kCapF64);
+    rc = upload_plan(ctx, ctx->pl_c, ctx->h_tmp.data(), m, mixed);
     if (rc) return rc;
-    if (mixed) {
-        rc = upload_items(ctx, ctx->it_c32, ctx->h_tmp.data(), m, kCapF32);
-        if (rc) return rc;
-    }
     std::vector<int32_t> ctp((size_t)k + 1, 0);
     if (k > 0) {
         CK(cudaMemcpyAsync(ctp.data(), ctx->ct_rp.p, 4 * ((size_t)k + 1), cudaMemcpyDeviceToHost, ctx->stream));
         CK(cudaStreamSynchronize(ctx->stream));
     }
-    rc = upload_items(ctx, ctx->it_ct, ctp.data(), k, kCapF64);
+    rc = upload_plan(ctx, ctx->pl_ct, ctp.data(), k, mixed);
     if (rc) return rc;
-    if (mixed) {
-        rc = upload_items(ctx, ctx->it_ct32, ctp.data(), k, kCapF32);
-        if (rc) return rc;
-    }
     // pivot block inverse and the Schur diagonal
     CK(cudaMemsetAsync(&c->regularised, 0, sizeof(int), ctx->stream));
     if (k > 0)
@@ -468,6 +511,7 @@ int renew_impl(help_pcg* ctx, const double* d_host) {
     ctx->stats.renew_ms = now_ms() - t0;
     ctx->stats.nnz_c = ctx->nnz_c;
     ctx->stats.pivots = k;
+    ctx->stats.dense_regularised = ctx->dense_regularised;
     return HELP_OK;
 }
 
@@ -513,6 +557,9 @@ int help_pcg_create(const help_pcg_options* opt, help_pcg** out) {
     if (e == cudaSuccess) e = ctx->ctrl.ensure(sizeof(DevCtrl));
     if (e == cudaSuccess) e = cudaMemset(ctx->ctrl.p, 0, sizeof(DevCtrl));
     if (e == cudaSuccess) e = ctx->partials.ensure(8 * (size_t)kPartElems);
+    if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev0);
+    if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev1);
+    if (e == cudaSuccess) e = cudaMallocHost((void**)&ctx->h_sc, sizeof(CgScalars));
     if (e != cudaSuccess) {
         release_all(ctx);
         if (ctx->stream) cudaStreamDestroy(ctx->stream);
@@ -531,6 +578,11 @@ void help_pcg_free(help_pcg* ctx) {
     ctx->ctrl.release();
     ctx->partials.release();
     if (ctx->h_stage) cudaFreeHost(ctx->h_stage);
+    for (int s = 0; s < 2; ++s)
+        if (ctx->graph_exec[s]) cudaGraphExecDestroy(ctx->graph_exec[s]);
+    if (ctx->h_sc) cudaFreeHost(ctx->h_sc);
+    if (ctx->ev0) cudaEventDestroy(ctx->ev0);
+    if (ctx->ev1) cudaEventDestroy(ctx->ev1);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
 }
@@ -590,24 +642,20 @@ int help_pcg_construct(help_pcg* ctx, int32_t m, int32_t n, const int32_t* col_p
     CK(cudaMemcpyAsync(ctx->ri.p, row_ind, 4 * (size_t)nnz, cudaMemcpyHostToDevice, ctx->stream));
     CK(cudaMemcpyAsync(ctx->avT.p, val, 8 * (size_t)nnz, cudaMemcpyHostToDevice, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
-    int rc = upload_items(ctx, ctx->it_csr, ctx->h_rp.data(), m, kCapF64);
-    if (!rc) rc = upload_items(ctx, ctx->it_csc, ctx->h_cp.data(), n, kCapF64);
-    if (!rc && mixed) rc = upload_items(ctx, ctx->it_csr32, ctx->h_rp.data(), m, kCapF32);
-    if (!rc && mixed) rc = upload_items(ctx, ctx->it_csc32, ctx->h_cp.data(), n, kCapF32);
+    int rc = upload_plan(ctx, ctx->pl_csr, ctx->h_rp.data(), m, mixed);
+    if (!rc) rc = upload_plan(ctx, ctx->pl_csc, ctx->h_cp.data(), n, mixed);
     if (!rc) rc = alloc_vectors(ctx);
     if (rc) return rc;
-    // persistent grid sizes (every block must be co-resident)
-    int per_sm = 0;
-    const size_t smem64 = std::max(spmv_smem_bytes<double>(kCapF64), (size_t)std::max(ctx->opt.pivots, 1) * 8);
-    CK(pcg_configure<double>(ctx->threads, smem64, &per_sm));
-    if (per_sm < 1) return fail(ctx, HELP_E_ARG, "construct: persistent kernel does not fit on an SM");
-    ctx->coop_blocks_f64 = per_sm * ctx->num_sms;
-    if (mixed) {
-        const size_t smem32 = std::max(spmv_smem_bytes<float>(kCapF32), (size_t)std::max(ctx->opt.pivots, 1) * 8);
-        CK(pcg_configure<float>(ctx->threads, smem32, &per_sm));
-        if (per_sm < 1) return fail(ctx, HELP_E_ARG, "construct: persistent kernel does not fit on an SM");
-        ctx->coop_blocks_f32 = per_sm * ctx->num_sms;
+    // CG kernels: grid-stride, grid sized to the work (small problems pay
+    // less for the per-block partial sums), at most 8 blocks per SM
+    {
+        const int64_t work = std::max<int64_t>(nnz, 32 * (int64_t)std::max(m, n));
+        const int64_t nb = (work + 16383) / 16384;
+        ctx->cg_blocks = (int)std::max<int64_t>(8, std::min<int64_t>(nb, (int64_t)ctx->num_sms * 8));
     }
+    CK(ctx->cg_part.ensure(sizeof(double) * 4 * (size_t)ctx->cg_blocks));
+    CK(cg_configure<double>(std::max(ctx->opt.pivots, 1)));
+    if (mixed) CK(cg_configure<float>(std::max(ctx->opt.pivots, 1)));
     ctx->constructed = true;
     ctx->renewed = false;
     return HELP_OK;
@@ -651,14 +699,17 @@ int help_pcg_solve(help_pcg* ctx, const double* d, const double* b_1, const doub
     }
     const double t0 = now_ms();
     const int m = ctx->m, n = ctx->n;
+    ctx->solve_kernel_ms = 0;
+    ctx->solve_iters_f32 = 0;
+    ctx->solve_launches = 0;
     rc = h2d(ctx, ctx->b1.as<double>(), b_1, n);
     if (!rc) rc = h2d(ctx, ctx->b2.as<double>(), b_2, m);
     if (rc) return rc;
     // u = D^-1/2 b_1 ;  rhs = B u - b_2 = A D^-1 b_1 - b_2   (UsePCG_CPU.cpp:103-112)
     CK(vec_scale_mul(ctx->s.as<double>(), ctx->b1.as<double>(), ctx->u.as<double>(), n, ctx->stream));
-    CK(spmv_launch<double>(kEpiRhs, ctx->it_csr.items(), ctx->it_csr.n, ctx->rp.as<int>(), ctx->ci.as<int>(),
-                           ctx->bv.as<double>(), ctx->it_csr.cap, ctx->u.as<double>(), ctx->rhs.as<double>(),
-                           ctx->b2.as<double>(), nullptr, nullptr, 0.0, 0, ctx->threads, ctx->stream));
+    CK(spmv_launch<double>(kEpiRhs, view<double>(ctx->pl_csr, ctx->rp, ctx->ci, ctx->bv), ctx->u.as<double>(),
+                           ctx->rhs.as<double>(), ctx->b2.as<double>(), nullptr, nullptr, 0.0, spmv_blocks(ctx),
+                           kSpmvThreads, ctx->stream));
     // x_2 (UsePCG_CPU.cpp:154-166)
     const bool warm = ctx->opt.warm_start && ctx->have_prev_x2;
     long long iters = 0;
@@ -671,9 +722,9 @@ int help_pcg_solve(help_pcg* ctx, const double* d, const double* b_1, const doub
     if (!rc) rc = sumsq_host(ctx, ctx->rhs.as<double>(), m, &rhs2);
     if (rc) return rc;
     // x_1 = D^-1 (b_1 - A^T x_2) = D^-1/2 (u - B^T x_2)   (UsePCG_CPU.cpp:171-177)
-    CK(spmv_launch<double>(kEpiBacksub, ctx->it_csc.items(), ctx->it_csc.n, ctx->cp.as<int>(), ctx->ri.as<int>(),
-                           ctx->bvT.as<double>(), ctx->it_csc.cap, ctx->x.as<double>(), ctx->x1.as<double>(),
-                           ctx->u.as<double>(), nullptr, ctx->s.as<double>(), 0.0, 0, ctx->threads, ctx->stream));
+    CK(spmv_launch<double>(kEpiBacksub, view<double>(ctx->pl_csc, ctx->cp, ctx->ri, ctx->bvT), ctx->x.as<double>(),
+                           ctx->x1.as<double>(), ctx->u.as<double>(), nullptr, ctx->s.as<double>(), 0.0,
+                           spmv_blocks(ctx), kSpmvThreads, ctx->stream));
     rc = d2h(ctx, x_1, ctx->x1.as<double>(), n);
     if (!rc) rc = d2h(ctx, x_2, ctx->x.as<double>(), m);
     if (rc) return rc;
@@ -686,6 +737,10 @@ int help_pcg_solve(help_pcg* ctx, const double* d, const double* b_1, const doub
     ctx->stats.rel_residual = rhs2 > 0.0 ? std::sqrt(rr / rhs2) : std::sqrt(rr);
     ctx->stats.solve_ms = now_ms() - t0;
     ctx->stats.solves++;
+    ctx->stats.cg_kernel_ms = ctx->solve_kernel_ms;
+    ctx->stats.cg_kernel_ms_total += ctx->solve_kernel_ms;
+    ctx->stats.cg_iterations_fp32 = ctx->solve_iters_f32;
+    ctx->stats.cg_launches = ctx->solve_launches;
     if (!converged && !ctx->opt.fallback) return fail(ctx, HELP_E_NOT_CONVERGED, "solve: iteration cap reached");
     return HELP_OK;
 }
@@ -701,36 +756,46 @@ const char* help_pcg_last_error(const help_pcg* ctx) { return ctx ? ctx->err.c_s
 int help_pcg_matvec_dev(help_pcg* ctx, int32_t op, int32_t fp32, const void* x, void* y, void* stream) {
     if (!ctx || !x || !y) return HELP_E_ARG;
     if (!ctx->constructed) return fail(ctx, HELP_E_ARG, "matvec: construct first");
-    if ((op == HELP_OP_ADAT || fp32) && !ctx->renewed) return fail(ctx, HELP_E_ARG, "matvec: renew first");
+    if ((op >= HELP_OP_ADAT || fp32) && !ctx->renewed) return fail(ctx, HELP_E_ARG, "matvec: renew first");
     if (fp32 && ctx->opt.precision != HELP_PREC_MIXED)
         return fail(ctx, HELP_E_ARG, "matvec: FP32 copy exists only with HELP_PREC_MIXED");
-    cudaStream_t st = stream ? (cudaStream_t)stream : ctx->stream;
-    const ItemList& icsr = fp32 ? ctx->it_csr32 : ctx->it_csr;
-    const ItemList& icsc = fp32 ? ctx->it_csc32 : ctx->it_csc;
+    cudaStream_t st = (cudaStream_t)stream;  // NULL: the legacy default stream
+    const int nb = spmv_blocks(ctx);
     if (op == HELP_OP_A || op == HELP_OP_AT) {
         if (fp32) return fail(ctx, HELP_E_ARG, "matvec: A / A^T only in FP64");
         const bool t = op == HELP_OP_AT;
-        const ItemList& L = t ? ctx->it_csc : ctx->it_csr;
-        CK(spmv_launch<double>(kEpiStore, L.items(), L.n, t ? ctx->cp.as<int>() : ctx->rp.as<int>(),
-                               t ? ctx->ri.as<int>() : ctx->ci.as<int>(), t ? ctx->avT.as<double>() : ctx->av.as<double>(),
-                               L.cap, (const double*)x, (double*)y, nullptr, nullptr, nullptr, 0.0, 0, ctx->threads, st));
+        const SpmvView<double> M = t ? view<double>(ctx->pl_csc, ctx->cp, ctx->ri, ctx->avT)
+                                     : view<double>(ctx->pl_csr, ctx->rp, ctx->ci, ctx->av);
+        CK(spmv_launch<double>(kEpiStore, M, (const double*)x, (double*)y, nullptr, nullptr, nullptr, 0.0, nb,
+                               kSpmvThreads, st));
+        return HELP_OK;
+    }
+    if (op == HELP_OP_B || op == HELP_OP_BT) {
+        const bool t = op == HELP_OP_BT;
+        if (fp32) {
+            const SpmvView<float> M = t ? view<float>(ctx->pl_csc, ctx->cp, ctx->ri, ctx->bvT32)
+                                        : view<float>(ctx->pl_csr, ctx->rp, ctx->ci, ctx->bv32);
+            CK(spmv_launch<float>(kEpiStore, M, (const float*)x, (float*)y, nullptr, nullptr, nullptr, 0.0, nb,
+                                  kSpmvThreads, st));
+        } else {
+            const SpmvView<double> M = t ? view<double>(ctx->pl_csc, ctx->cp, ctx->ri, ctx->bvT)
+                                         : view<double>(ctx->pl_csr, ctx->rp, ctx->ci, ctx->bv);
+            CK(spmv_launch<double>(kEpiStore, M, (const double*)x, (double*)y, nullptr, nullptr, nullptr, 0.0, nb,
+                                   kSpmvThreads, st));
+        }
         return HELP_OK;
     }
     if (op != HELP_OP_ADAT) return fail(ctx, HELP_E_ARG, "matvec: unknown op");
     if (fp32) {
-        CK(spmv_launch<float>(kEpiStore, icsc.items(), icsc.n, ctx->cp.as<int>(), ctx->ri.as<int>(),
-                              ctx->bvT32.as<float>(), icsc.cap, (const float*)x, ctx->t32.as<float>(), nullptr, nullptr,
-                              nullptr, 0.0, 0, ctx->threads, st));
-        CK(spmv_launch<float>(kEpiAddDelta, icsr.items(), icsr.n, ctx->rp.as<int>(), ctx->ci.as<int>(),
-                              ctx->bv32.as<float>(), icsr.cap, ctx->t32.as<float>(), (float*)y, (const float*)x,
-                              nullptr, nullptr, ctx->opt.delta, 0, ctx->threads, st));
+        CK(spmv_launch<float>(kEpiStore, view<float>(ctx->pl_csc, ctx->cp, ctx->ri, ctx->bvT32), (const float*)x,
+                              ctx->t32.as<float>(), nullptr, nullptr, nullptr, 0.0, nb, kSpmvThreads, st));
+        CK(spmv_launch<float>(kEpiAddDelta, view<float>(ctx->pl_csr, ctx->rp, ctx->ci, ctx->bv32), ctx->t32.as<float>(),
+                              (float*)y, (const float*)x, nullptr, nullptr, ctx->opt.delta, nb, kSpmvThreads, st));
     } else {
-        CK(spmv_launch<double>(kEpiStore, icsc.items(), icsc.n, ctx->cp.as<int>(), ctx->ri.as<int>(),
-                               ctx->bvT.as<double>(), icsc.cap, (const double*)x, ctx->t.as<double>(), nullptr,
-                               nullptr, nullptr, 0.0, 0, ctx->threads, st));
-        CK(spmv_launch<double>(kEpiAddDelta, icsr.items(), icsr.n, ctx->rp.as<int>(), ctx->ci.as<int>(),
-                               ctx->bv.as<double>(), icsr.cap, ctx->t.as<double>(), (double*)y, (const double*)x,
-                               nullptr, nullptr, ctx->opt.delta, 0, ctx->threads, st));
+        CK(spmv_launch<double>(kEpiStore, view<double>(ctx->pl_csc, ctx->cp, ctx->ri, ctx->bvT), (const double*)x,
+                               ctx->t.as<double>(), nullptr, nullptr, nullptr, 0.0, nb, kSpmvThreads, st));
+        CK(spmv_launch<double>(kEpiAddDelta, view<double>(ctx->pl_csr, ctx->rp, ctx->ci, ctx->bv), ctx->t.as<double>(),
+                               (double*)y, (const double*)x, nullptr, nullptr, ctx->opt.delta, nb, kSpmvThreads, st));
     }
     return HELP_OK;
 }
@@ -739,11 +804,11 @@ int help_pcg_matvec(help_pcg* ctx, int32_t op, const double* x, double* y) {
     if (!ctx || !x || !y) return HELP_E_ARG;
     if (!ctx->constructed) return fail(ctx, HELP_E_ARG, "matvec: construct first");
     CK(cudaSetDevice(ctx->device));
-    const size_t nin = (op == HELP_OP_A) ? ctx->n : ctx->m;
-    const size_t nout = (op == HELP_OP_AT) ? ctx->n : ctx->m;
+    const size_t nin = (op == HELP_OP_A || op == HELP_OP_B) ? ctx->n : ctx->m;
+    const size_t nout = (op == HELP_OP_AT || op == HELP_OP_BT) ? ctx->n : ctx->m;
     int rc = h2d(ctx, ctx->xacc.as<double>(), x, nin);
     if (rc) return rc;
-    rc = help_pcg_matvec_dev(ctx, op, 0, ctx->xacc.p, ctx->res.p, nullptr);
+    rc = help_pcg_matvec_dev(ctx, op, 0, ctx->xacc.p, ctx->res.p, (void*)ctx->stream);
     if (rc) return rc;
     return d2h(ctx, y, ctx->res.as<double>(), nout);
 }

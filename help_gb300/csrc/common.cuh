@@ -1,5 +1,5 @@
-// Device-side building blocks shared by the kernels: bounded grid barrier,
-// deterministic block reductions, cache-hinted loads.
+// Device-side building blocks shared by the kernels: deterministic block
+// reductions, cache-hinted loads.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -34,71 +34,28 @@ constexpr int kStatusOk = 0;
 constexpr int kStatusTimeout = -5;
 constexpr int kStatusNumeric = -4;
 
-// Grid-wide barrier for cooperative launches (all blocks co-resident).
-// Generation-counting: the last block to arrive resets the counter and bumps
-// the generation; the others spin on the generation with a wall-clock limit.
-// On timeout, or when another block already gave up, the barrier returns
-// false and the caller must return from the kernel.  The limit bounds every
-// wait, so a faulty phase ends the kernel with an error status instead of a
-// hang.
-struct GridBarrier {
-    unsigned int* count;
-    unsigned int* gen;
-    int* status;  // 0 ok, < 0 error (set once)
-};
-
-constexpr uint64_t kBarrierTimeoutNs = 2000000000ull;  // 2 s
-
-HELP_DEVINL bool grid_sync(const GridBarrier& b) {
-    __shared__ int s_ok;
+// Deterministic block-wide sum with few FP64 instructions (GB300 issues FP64
+// at ~2 lanes/clk/SM, so a reduction where every thread adds every warp's
+// partial costs microseconds): a shared-memory tree halving the active
+// threads, then one warp's shuffles.  blockDim.x must be a power of two
+// <= 1024; `red` holds blockDim.x doubles.  Result valid in every thread.
+HELP_DEVINL double block_sum(double v, double* red) {
+    const int tid = threadIdx.x;
     __syncthreads();
-    if (threadIdx.x == 0) {
-        volatile unsigned int* vgen = b.gen;
-        volatile int* vstat = b.status;
-        const unsigned int g = *vgen;
-        __threadfence();
-        const unsigned int arrived = atomicAdd(b.count, 1u) + 1u;
-        int ok = 1;
-        if (arrived == gridDim.x) {
-            atomicExch(b.count, 0u);
-            __threadfence();
-            atomicAdd(b.gen, 1u);
-        } else {
-            const uint64_t t0 = globaltimer_ns();
-            while (*vgen == g) {
-                if (*vstat != 0) {
-                    ok = 0;
-                    break;
-                }
-                if (globaltimer_ns() - t0 > kBarrierTimeoutNs) {
-                    atomicCAS(b.status, 0, kStatusTimeout);
-                    ok = 0;
-                    break;
-                }
-                __nanosleep(32);
-            }
-        }
-        __threadfence();
-        if (*vstat != 0) ok = 0;
-        s_ok = ok;
+    red[tid] = v;
+    __syncthreads();
+    for (int s = blockDim.x >> 1; s >= 32; s >>= 1) {
+        if (tid < s) red[tid] += red[tid + s];
+        __syncthreads();
+    }
+    if (tid < 32) {
+        double w = red[tid];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) w += __shfl_xor_sync(0xffffffffu, w, o);
+        if (tid == 0) red[0] = w;
     }
     __syncthreads();
-    return s_ok != 0;
-}
-
-// Deterministic block-wide sum (fixed tree for a fixed blockDim).  `red` must
-// hold blockDim.x / 32 doubles.  Result valid in every thread.
-HELP_DEVINL double block_sum(double v, double* red) {
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    __syncthreads();
-    if (lane == 0) red[warp] = v;
-    __syncthreads();
-    double s = 0.0;
-    for (int w = 0; w < nw; ++w) s += red[w];
-    __syncthreads();
-    return s;
+    return red[0];
 }
 
 template <class T>

@@ -9,6 +9,7 @@
 
 #include "../../include/help_gpu.h"
 #include "items.h"
+#include "kernels.h"
 
 namespace help {
 
@@ -37,12 +38,19 @@ struct DevMem {
     }
 };
 
-struct ItemList {
-    DevMem buf;
-    int32_t n = 0;
-    int32_t cap = 0;
-    const int4* items() const { return buf.as<int4>(); }
+// A planned CSR matrix: the split of its rows for spmv_rows (spmv.cuh), one
+// per precision (the group-size floor differs).
+struct RowSplit {
+    DevMem med, lng;
+    int32_t G = 1, short_max = 32, n_med = 0, n_long = 0;
 };
+struct RowPlan {
+    int32_t rows = 0;
+    RowSplit s64, s32;
+};
+
+constexpr int kGminF64 = 2;  // 2 lanes x 8 B = a 16-byte run per load, sector reuse through L1
+constexpr int kGminF32 = 8;  // 8 lanes x 4 B = one 32-byte sector per load
 
 // Results the persistent CG kernel leaves behind.
 struct CgOut {
@@ -68,9 +76,8 @@ struct Ctrl {
     int scratch[2];
 };
 
-constexpr int kCapF64 = 2048;   // nonzeros per SpMV work item (FP64 staging: 32 KB)
-constexpr int kCapF32 = 4096;   // (FP32 staging: 32 KB)
 constexpr int kTopkBins = 256;
+constexpr int kGraphIters = 8;    // CG iterations per graph launch
 
 }  // namespace help
 
@@ -91,8 +98,7 @@ struct help_pcg {
     help::DevMem cp, ri, avT;         // CSR(A^T) = CSC(A), original values
     help::DevMem bv, bvT;             // B = A D^-1/2 (FP64)
     help::DevMem bv32, bvT32;         // B in FP32 (mixed precision)
-    help::ItemList it_csr, it_csc;    // FP64 plans
-    help::ItemList it_csr32, it_csc32;  // FP32 plans
+    help::RowPlan pl_csr, pl_csc;     // row splits of A and A^T
 
     // renew state
     int32_t k = 0;
@@ -103,7 +109,7 @@ struct help_pcg {
     help::DevMem cr_cnt;                  // per row: entries of G[i,P]
     help::DevMem c_rp, c_ci, c_v, c_v32;  // C = G[non-pivot rows, P], CSR over all m rows
     help::DevMem ct_rp, ct_ci, ct_v, ct_v32, ct_blk;  // C^T, CSR over k rows
-    help::ItemList it_c, it_ct, it_c32, it_ct32;
+    help::RowPlan pl_c, pl_ct;
     help::DevMem g11, W, lwork;           // pivot block, its inverse, factor workspace
     std::vector<int32_t> h_tmp;
     int32_t dense_regularised = 0;
@@ -124,5 +130,15 @@ struct help_pcg {
     bool have_prev_x2 = false;
     help_pcg_stats stats{};
     int coop_blocks_f64 = 0, coop_blocks_f32 = 0;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    // CG graphs (one per precision), re-captured when their arguments change
+    cudaGraphExec_t graph_exec[2] = {nullptr, nullptr};
+    std::vector<unsigned char> graph_args[2];
+    int cg_blocks = 0;
+    help::DevMem cg_part;  // 4 x cg_blocks doubles
+    help::CgScalars* h_sc = nullptr;  // pinned mirror of the device scalars
+    double solve_kernel_ms = 0;       // accumulators for the current solve
+    long long solve_iters_f32 = 0;
+    int solve_launches = 0;
     int threads = 512;
 };

@@ -1,41 +1,36 @@
-// Host-side planning of SpMV work items for one CSR matrix (see spmv.cuh).
+// Host-side planning of one CSR matrix for spmv_rows (spmv.cuh).
 //
-// Rows longer than `cap` become single-row items (processed CTA-wide) and are
-// listed first so they start early; the other rows are packed in order into
-// blocks of consecutive rows with at most `cap` nonzeros and at most
-// `max_rows` rows each.  Items are int4 {row0, row1 | flags, e0, e1}.
+// G, the number of lanes that share a short row, is the smallest power of two
+// (at least g_min, at most 32) giving each lane at most ~8 nonzeros of an
+// average row.  Rows up to 32 G nonzeros are short; rows up to kLongRowMin
+// are taken one warp each; longer rows one CTA each.  Medium and long rows are
+// listed explicitly.
 #include "items.h"
-
-#include <algorithm>
 
 namespace help {
 
-std::vector<Int4> plan_items(const int32_t* ptr, int32_t rows, int32_t cap, int32_t max_rows,
-                             int32_t thread_row_max) {
-    std::vector<Int4> longs, shorts;
-    int32_t start = -1;
-    bool has_long = false;
-    auto close = [&](int32_t end_row) {
-        if (start >= 0) {
-            shorts.push_back({start, end_row | (has_long ? kItemHasLongRowsHost : 0), ptr[start], ptr[end_row]});
-            start = -1;
-            has_long = false;
-        }
-    };
+RowPlanHost plan_rows(const int32_t* ptr, int32_t rows, int32_t g_min) {
+    RowPlanHost p;
+    int64_t tot = 0, cnt = 0;
     for (int32_t i = 0; i < rows; ++i) {
         const int32_t len = ptr[i + 1] - ptr[i];
-        if (len > cap) {
-            close(i);
-            longs.push_back({i, i + 1, ptr[i], ptr[i + 1]});
-            continue;
+        if (len <= kLongRowMin) {
+            tot += len;
+            ++cnt;
         }
-        if (start >= 0 && (ptr[i + 1] - ptr[start] > cap || i - start >= max_rows)) close(i);
-        if (start < 0) start = i;
-        if (len > thread_row_max) has_long = true;
     }
-    close(rows);
-    longs.insert(longs.end(), shorts.begin(), shorts.end());
-    return longs;
+    const double avg = cnt ? (double)tot / (double)cnt : 0.0;
+    int32_t G = 1;
+    while (G < g_min) G *= 2;
+    while (G < 32 && G * 8 < avg) G *= 2;
+    p.G = G;
+    p.short_max = 32 * G;
+    for (int32_t i = 0; i < rows; ++i) {
+        const int32_t len = ptr[i + 1] - ptr[i];
+        if (len > kLongRowMin) p.lng.push_back(i);
+        else if (len > p.short_max) p.med.push_back(i);
+    }
+    return p;
 }
 
 }  // namespace help

@@ -5,14 +5,16 @@
 
 namespace help {
 
-struct Int4 {
-    int32_t x, y, z, w;
+// Host-side split of the rows of one CSR matrix for spmv_rows (spmv.cuh).
+struct RowPlanHost {
+    int32_t G = 1;          // lanes per short row
+    int32_t short_max = 32; // longer rows are medium or long
+    std::vector<int32_t> med, lng;
 };
-static_assert(sizeof(Int4) == 16, "Int4 must match the device int4 layout");
 
-constexpr int32_t kItemHasLongRowsHost = 1 << 30;  // must equal kItemHasLongRows (spmv.cuh)
+constexpr int32_t kLongRowMin = 4096;  // rows above this length take a whole CTA
 
-std::vector<Int4> plan_items(const int32_t* ptr, int32_t rows, int32_t cap, int32_t max_rows,
-                             int32_t thread_row_max);
+// g_min: smallest group (so one group's loads span a 32-byte sector).
+RowPlanHost plan_rows(const int32_t* ptr, int32_t rows, int32_t g_min);
 
 }  // namespace help

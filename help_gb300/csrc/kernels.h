@@ -6,6 +6,7 @@
 #include <stdint.h>
 
 #include "common.cuh"
+#include "spmv.cuh"
 
 namespace help {
 
@@ -16,57 +17,35 @@ struct TopkStateDev {
     int n_greater;              // rows strictly above the threshold
 };
 
-struct CgOutDev {
-    long long iterations;
-    double rr0;
-    double rr;
-    int converged;
+// Device-side scalars of one CG run (one set per context).
+struct CgScalars {
+    double rr0, rr, term2, rz, rz_old, alpha, beta;
+    double tol2;          // set by the host: stop when r.r < tol2 * r0.r0
+    long long it;
+    long long max_iter;   // set by the host
+    int done;             // 0 running, 1 converged, 2 iteration cap, 3 breakdown
     int status;
-    int final_buf;
-    int pad;
+    unsigned int ticket[4];
 };
 
 // Device control block (one per context).
 struct DevCtrl {
-    unsigned int bar_count;
-    unsigned int bar_gen;
     int status;
     int regularised;
-    CgOutDev cg;
+    CgScalars cg;
     TopkStateDev topk;
     int totals[8];
 };
 
 template <class V>
-struct PcgArgs {
-    int m, n, k, cap;
-    const int4* csr_items;
-    int n_csr;
-    const int* rp;
-    const int* ci;
-    const V* bv;
-    const int4* csc_items;
-    int n_csc;
-    const int* cp;
-    const int* ri;
-    const V* bvT;
-    const int4* c_items;
-    int n_c;
-    const int* c_rp;
-    const int* c_ci;
-    const V* c_v;
-    const int4* ct_items;
-    int n_ct;
-    const int* ct_rp;
-    const int* ct_ci;
-    const V* ct_v;
+struct CgArgs {
+    int m, n, k;
+    SpmvView<V> csr, csc, c, ct;  // B, B^T, C = G[N, P], C^T
     const int* piv;
     const int* pivpos;
     const double* W;
     const V* dsinv;
     double delta;
-    double tol2;
-    long long max_iter;
     V* x;
     V* r0;
     V* r1;
@@ -77,16 +56,21 @@ struct PcgArgs {
     V* t;
     double* a;
     double* w;
-    double* part;  // 3 * gridDim doubles
+    double* part_rr;  // gridDim doubles each
+    double* part_rz;
+    double* part_aw;
+    double* part_pq;
     int precond_only;  // stop after the first preconditioner application (z in p1)
-    GridBarrier bar;
-    CgOutDev* out;
+    CgScalars* sc;
 };
 
 template <class V>
-cudaError_t pcg_configure(int threads, size_t smem, int* blocks_per_sm);
+cudaError_t cg_configure(int k_max);
 template <class V>
-cudaError_t pcg_launch(const PcgArgs<V>& args, int blocks, int threads, size_t smem, cudaStream_t stream);
+cudaError_t cg_launch_init(const CgArgs<V>& A, int blocks, cudaStream_t st);
+template <class V>
+cudaError_t cg_launch_iteration(const CgArgs<V>& A, int blocks, cudaStream_t st);
+int cg_threads();
 
 // ---- standalone SpMV over items (vec.cu)
 enum SpmvEpi {
@@ -97,9 +81,8 @@ enum SpmvEpi {
     kEpiAddDelta = 4   // y[row] = s + delta * aux[row]
 };
 template <class V>
-cudaError_t spmv_launch(int epi, const int4* items, int n_items, const int* ptr, const int* idx, const V* val,
-                        int cap, const V* x, V* y, const V* aux, const V* aux2, const double* s2, double delta,
-                        int blocks, int threads, cudaStream_t stream);
+cudaError_t spmv_launch(int epi, const SpmvView<V>& M, const V* x, V* y, const V* aux, const V* aux2,
+                        const double* s2, double delta, int blocks, int threads, cudaStream_t stream);
 
 // ---- vector kernels (vec.cu)
 cudaError_t vec_scale_mul(const double* a, const double* b, double* out, int64_t n, cudaStream_t st);  // out = a*b

@@ -1,245 +1,333 @@
-// Persistent preconditioned conjugate gradient on G x = b, G = B B^T + delta I,
+// Preconditioned conjugate gradient on G x = b, G = B B^T + delta I,
 // B = A D^-1/2 -- the loop of ConjugateGradient (PCG.cpp:296-395) with the
 // partial-Cholesky preconditioner of PCG.cpp:183-196 applied in block form.
 //
-// One cooperative launch runs the whole solve: every block stays resident,
-// phases are separated by a bounded grid barrier, and every scalar (alpha,
-// beta, the stopping test) is formed by every block from the same per-block
-// partial sums in the same order, so all blocks take identical decisions and
-// the run is bitwise reproducible.
+// Each iteration is six kernels, captured once into a CUDA graph that runs
+// several iterations per launch; the host only polls a device flag between
+// graph launches.  Scalars (alpha, beta, the stopping test) are formed on the
+// device: every kernel that ends a reduction has each block write its partial
+// sum, and the last block to finish (ticket counter) adds the partials in
+// block order -- so the run is deterministic -- and publishes the scalar for
+// the next kernel.  Every kernel first reads the `done` flag and returns at
+// once when the solve has finished, so a graph launched past convergence
+// costs only empty launches.  No kernel waits on another block.
 //
-// Preconditioner M = [L11 0; L21 I] diag(D1, D_S) [L11 0; L21 I]^T restricted
-// to the pivot rows P (k of them) is applied without the dense L21 the
-// reference materialises (PCG.cpp:143-155).  With C = G[N, P] (N = non-pivot
-// rows) and W = G11^-1:
-//     a   = W r_P
+// Preconditioner M = [L11 0; L21 I] diag(D1, D_S) [L11 0; L21 I]^T on the k
+// pivot rows P is applied without the dense L21 the reference materialises
+// (PCG.cpp:143-155).  With C = G[N, P] (N = non-pivot rows), W = G11^-1:
+//     a   = W r_P            (end of the previous iteration)
 //     z_N = D_S^-1 (r_N - C a)
 //     w   = r_P - C^T z_N
 //     z_P = W w
-// and r_P . z_P = a . w (W symmetric), so beta is known in the same phase that
-// forms the new search direction.  Per iteration:
-//   P2: z_N, r_N.z_N          | P3: w          | P4: beta, z_P, p_new
-//   A : t = B^T p_new         | B : q = B t + delta p_new, p.q
-//   C : alpha, x += alpha p, r -= alpha q, r.r, a = W r_P
+// and r_P . z_P = a . w (W symmetric), so beta is known before p is formed.
+//   k_p2 : z_N, r_N.z_N                      k_p3 : w, a.w  -> rz, beta
+//   k_p4 : z_P, p_new = z + beta p           k_a  : t = B^T p_new
+//   k_b  : q = B t + delta p_new, p.q -> alpha
+//   k_c  : x += alpha p, r -= alpha q, r.r -> stop?, a = W r_P
 // Vectors are V (double, or float for the inner solves of mixed precision);
 // dot products, alpha/beta and the pivot-block work stay in double.
-#include <cooperative_groups.h>
-
 #include "common.cuh"
 #include "kernels.h"
 #include "spmv.cuh"
 
 namespace help {
 
+namespace {
+
+constexpr int kCgThreads = 256;
+
+// Sum of the per-block partials (in block order) by the calling block.
+HELP_DEVINL double sum_parts(const double* p, const double* p2, int nb, double* red) {
+    double s = 0.0;
+    for (int b = threadIdx.x; b < nb; b += blockDim.x) s += p2 ? p[b] + p2[b] : p[b];
+    return block_sum(s, red);
+}
+
+// Writes this block's partial and returns true in the last block to finish.
+HELP_DEVINL bool publish_partial(double v, double* part, unsigned int* ticket) {
+    __shared__ int s_last;
+    if (threadIdx.x == 0) {
+        part[blockIdx.x] = v;
+        __threadfence();
+        const unsigned int t = atomicAdd(ticket, 1u);
+        s_last = (t == gridDim.x - 1);
+    }
+    __syncthreads();
+    if (s_last) __threadfence();
+    return s_last != 0;
+}
+
+HELP_DEVINL bool cg_done(const CgScalars* sc) { return *(volatile const int*)&sc->done != 0; }
+
+// out(c, (W y)_c) for the rows c of W owned by this block's warps (k x k, row-major).
+template <class YF, class OUT>
+HELP_DEVINL void gemv_rows(int k, const double* __restrict__ W, const YF& yf, const OUT& out, double* s_vec) {
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = blockDim.x >> 5;
+    const bool active = (long long)blockIdx.x * nw < k;
+    if (active)
+        for (int c = tid; c < k; c += blockDim.x) s_vec[c] = yf(c);
+    __syncthreads();
+    if (active) {
+        for (int c = blockIdx.x * nw + warp; c < k; c += gridDim.x * nw) {
+            const double* Wr = W + (size_t)c * k;
+            double acc = 0.0;
+            for (int c2 = lane; c2 < k; c2 += 32) acc = fma(ld_ro(Wr + c2), s_vec[c2], acc);
+            acc = warp_sum(acc);
+            if (lane == 0) out(c, acc);
+        }
+    }
+    __syncthreads();
+}
+
+// ---- initial: r.r and a = W r_P of the starting residual (buffer 0)
 template <class V>
-__global__ void __launch_bounds__(512) pcg_persistent(const __grid_constant__ PcgArgs<V> A) {
+__global__ void __launch_bounds__(kCgThreads) k_init(const CgArgs<V> A) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    V* s_val = reinterpret_cast<V*>(smem_raw);
-    V* s_x = s_val + A.cap;
     double* s_vec = reinterpret_cast<double*>(smem_raw);
-    __shared__ double red[32];
-
-    const int G = gridDim.x, bid = blockIdx.x, tid = threadIdx.x, T = blockDim.x;
-    const int lane = tid & 31, warp = tid >> 5, nw = T >> 5;
-    const long long gtid = (long long)bid * T + tid, gthr = (long long)G * T;
-    double* part_rr = A.part;
-    double* part_rz = A.part + G;
-    double* part_pq = A.part + 2 * G;
-
-    auto sum_parts = [&](const double* p) {
-        double s = 0.0;
-        for (int b = tid; b < G; b += T) s += p[b];
-        return block_sum(s, red);
-    };
-    // out(c, (W y)_c) for the rows c of W owned by this block's warps.
-    auto gemv = [&](auto yf, auto out) {
-        const bool active = (long long)bid * nw < A.k;
-        if (active)
-            for (int c = tid; c < A.k; c += T) s_vec[c] = yf(c);
-        __syncthreads();
-        if (active) {
-            for (int c = bid * nw + warp; c < A.k; c += G * nw) {
-                const double* Wr = A.W + (size_t)c * A.k;
-                double acc = 0.0;
-                for (int c2 = lane; c2 < A.k; c2 += 32) acc = fma(ld_ro(Wr + c2), s_vec[c2], acc);
-                acc = warp_sum(acc);
-                if (lane == 0) out(c, acc);
+    __shared__ double red[kCgThreads];
+    const V* r = A.r0;
+    double rr = 0.0;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < A.m; i += (long long)gridDim.x * blockDim.x) {
+        const double v = (double)r[i];
+        rr = fma(v, v, rr);
+    }
+    rr = block_sum(rr, red);
+    gemv_rows(A.k, A.W, [&](int c) { return (double)r[A.piv[c]]; }, [&](int c, double s) { A.a[c] = s; }, s_vec);
+    if (publish_partial(rr, A.part_rr, &A.sc->ticket[0])) {
+        const double tot = sum_parts(A.part_rr, nullptr, gridDim.x, red);
+        if (threadIdx.x == 0) {
+            CgScalars* sc = A.sc;
+            sc->ticket[0] = 0;
+            sc->rr0 = tot;
+            sc->rr = tot;
+            sc->term2 = tot * sc->tol2;
+            sc->it = 0;
+            sc->status = 0;
+            if (!(tot == tot)) {
+                sc->status = kStatusNumeric;
+                sc->done = 3;
+            } else if (tot == 0.0 || sc->max_iter <= 0) {
+                sc->done = (tot == 0.0) ? 1 : 2;
+            } else {
+                sc->done = 0;
             }
         }
-        __syncthreads();
-    };
-
-    // ---- I0: r.r of the initial residual, a = W r_P
-    {
-        const V* r = A.r0;
-        double rr = 0.0;
-        for (long long i = gtid; i < A.m; i += gthr) {
-            const double v = (double)r[i];
-            rr = fma(v, v, rr);
-        }
-        rr = block_sum(rr, red);
-        if (tid == 0) part_rr[bid] = rr;
-        gemv([&](int c) { return (double)r[A.piv[c]]; }, [&](int c, double s) { A.a[c] = s; });
-        if (!grid_sync(A.bar)) return;
     }
-    const double rr0 = sum_parts(part_rr);
-    const double term2 = rr0 * A.tol2;
-    double rr = rr0, rz_old = 0.0;
-    long long it = 0;
-    int cur = 0, converged = 0, status = 0;
+}
 
-    for (;;) {
-        if (it > 0) rr = sum_parts(part_rr);
-        if (!(rr == rr)) {
-            status = kStatusNumeric;
-            break;
-        }
-        if (rr < term2 || rr == 0.0) {
-            converged = 1;
-            break;
-        }
-        if (it >= A.max_iter) break;
-        V* r = cur ? A.r1 : A.r0;
-        V* rn = cur ? A.r0 : A.r1;
-        V* p = cur ? A.p1 : A.p0;
-        V* pn = cur ? A.p0 : A.p1;
-
-        // ---- P2: z_N = D_S^-1 (r_N - C a), partial r_N . z_N
-        {
-            double rz = 0.0;
-            spmv_items<V>(
-                A.c_items, A.n_c, bid, G, A.c_rp, A.c_ci, A.c_v, A.cap, [&](int c) { return (V)A.a[c]; },
-                [&](int i, V s) {
-                    if (A.pivpos[i] < 0) {
-                        const V ri = r[i];
-                        const V zi = A.dsinv[i] * (ri - s);
-                        A.z[i] = zi;
-                        rz = fma((double)ri, (double)zi, rz);
-                    }
-                },
-                s_val, s_x, red);
-            rz = block_sum(rz, red);
-            if (tid == 0) part_rz[bid] = rz;
-            if (!grid_sync(A.bar)) return;
-        }
-        // ---- P3: w = r_P - C^T z_N
-        spmv_items<V>(
-            A.ct_items, A.n_ct, bid, G, A.ct_rp, A.ct_ci, A.ct_v, A.cap, [&](int i) { return A.z[i]; },
-            [&](int c, V s) { A.w[c] = (double)r[A.piv[c]] - (double)s; }, s_val, s_x, red);
-        if (!grid_sync(A.bar)) return;
-
-        // ---- P4: rz = r_N.z_N + a.w, beta, z_P = W w, p_new = z + beta p
-        double rz;
-        {
-            double aw = 0.0;
-            for (int c = tid; c < A.k; c += T) aw = fma(A.a[c], A.w[c], aw);
-            aw = block_sum(aw, red);
-            rz = sum_parts(part_rz) + aw;
-        }
-        if (!(rz > 0.0)) {  // M^-1 not positive on r, or NaN
-            status = kStatusNumeric;
-            break;
-        }
-        const double beta = (it == 0) ? 0.0 : rz / rz_old;
-        const V vb = (V)beta;
-        const bool first = (it == 0);
-        gemv([&](int c) { return A.w[c]; },
-             [&](int c, double s) {
-                 const int i = A.piv[c];
-                 const V zc = (V)s;
-                 pn[i] = first ? zc : fma_t(vb, p[i], zc);
-             });
-        for (long long i = gtid; i < A.m; i += gthr) {
+// ---- P2: z_N = D_S^-1 (r_N - C a), partial r_N . z_N
+template <class V>
+__global__ void __launch_bounds__(kCgThreads) k_p2(const CgArgs<V> A) {
+    if (cg_done(A.sc)) return;
+    __shared__ double red[kCgThreads];
+    const V* r = (A.sc->it & 1) ? A.r1 : A.r0;
+    double rz = 0.0;
+    spmv_rows<V>(
+        A.c, [&](int c) { return (V)A.a[c]; },
+        [&](int i, V s) {
             if (A.pivpos[i] < 0) {
-                const V zi = A.z[i];
-                pn[i] = first ? zi : fma_t(vb, p[i], zi);
+                const V ri = r[i];
+                const V zi = A.dsinv[i] * (ri - s);
+                A.z[i] = zi;
+                rz = fma((double)ri, (double)zi, rz);
+            }
+        },
+        red);
+    rz = block_sum(rz, red);
+    if (threadIdx.x == 0) A.part_rz[blockIdx.x] = rz;
+}
+
+// ---- P3: w = r_P - C^T z_N, partial a . w; last block: rz, beta
+template <class V>
+__global__ void __launch_bounds__(kCgThreads) k_p3(const CgArgs<V> A) {
+    if (cg_done(A.sc)) return;
+    __shared__ double red[kCgThreads];
+    const V* r = (A.sc->it & 1) ? A.r1 : A.r0;
+    double aw = 0.0;
+    spmv_rows<V>(
+        A.ct, [&](int i) { return A.z[i]; },
+        [&](int c, V s) {
+            const double wc = (double)r[A.piv[c]] - (double)s;
+            A.w[c] = wc;
+            aw = fma(A.a[c], wc, aw);
+        },
+        red);
+    aw = block_sum(aw, red);
+    if (publish_partial(aw, A.part_aw, &A.sc->ticket[1])) {
+        // k_p2 ran with the same grid, so part_rz holds gridDim.x partials too
+        const double rz = sum_parts(A.part_rz, A.part_aw, gridDim.x, red);
+        if (threadIdx.x == 0) {
+            CgScalars* sc = A.sc;
+            sc->ticket[1] = 0;
+            if (!(rz > 0.0)) {  // M^-1 not positive on r, or NaN
+                sc->status = kStatusNumeric;
+                sc->done = 3;
+            } else {
+                sc->beta = (sc->it == 0) ? 0.0 : rz / sc->rz_old;
+                sc->rz = rz;
             }
         }
-        if (!grid_sync(A.bar)) return;
-        if (A.precond_only) break;
-
-        // ---- A: t = B^T p_new
-        spmv_items<V>(
-            A.csc_items, A.n_csc, bid, G, A.cp, A.ri, A.bvT, A.cap, [&](int i) { return pn[i]; },
-            [&](int j, V s) { A.t[j] = s; }, s_val, s_x, red);
-        if (!grid_sync(A.bar)) return;
-
-        // ---- B: q = B t + delta p_new, partial p.q
-        {
-            double pq = 0.0;
-            const V vd = (V)A.delta;
-            const bool has_delta = (A.delta != 0.0);
-            spmv_items<V>(
-                A.csr_items, A.n_csr, bid, G, A.rp, A.ci, A.bv, A.cap, [&](int j) { return A.t[j]; },
-                [&](int i, V s) {
-                    const V pi = pn[i];
-                    const V qi = has_delta ? fma_t(vd, pi, s) : s;
-                    A.q[i] = qi;
-                    pq = fma((double)pi, (double)qi, pq);
-                },
-                s_val, s_x, red);
-            pq = block_sum(pq, red);
-            if (tid == 0) part_pq[bid] = pq;
-            if (!grid_sync(A.bar)) return;
-        }
-
-        // ---- C: alpha, x += alpha p, r -= alpha q, r.r, a = W r_P
-        {
-            const double pq = sum_parts(part_pq);
-            if (!(pq > 0.0)) {  // G not positive on p (breakdown) or NaN
-                status = kStatusNumeric;
-                break;
-            }
-            const double alpha = rz / pq;
-            const V va = (V)alpha;
-            double rrl = 0.0;
-            for (long long i = gtid; i < A.m; i += gthr) {
-                const V pi = pn[i], qi = A.q[i];
-                A.x[i] = fma_t(va, pi, A.x[i]);
-                const V ri = fma_t(-va, qi, r[i]);
-                rn[i] = ri;
-                rrl = fma((double)ri, (double)ri, rrl);
-            }
-            rrl = block_sum(rrl, red);
-            if (tid == 0) part_rr[bid] = rrl;
-            gemv([&](int c) {
-                     const int i = A.piv[c];
-                     return (double)fma_t(-va, A.q[i], r[i]);
-                 },
-                 [&](int c, double s) { A.a[c] = s; });
-            if (!grid_sync(A.bar)) return;
-        }
-        rz_old = rz;
-        cur ^= 1;
-        ++it;
     }
-    if (bid == 0 && tid == 0) {
-        A.out->iterations = it;
-        A.out->rr0 = rr0;
-        A.out->rr = rr;
-        A.out->converged = converged;
-        A.out->status = status;
-        A.out->final_buf = cur;
+}
+
+// ---- P4: z_P = W w, p_new = z + beta p
+template <class V>
+__global__ void __launch_bounds__(kCgThreads) k_p4(const CgArgs<V> A) {
+    if (cg_done(A.sc)) return;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    double* s_vec = reinterpret_cast<double*>(smem_raw);
+    const long long it = A.sc->it;
+    const V* p = (it & 1) ? A.p1 : A.p0;
+    V* pn = (it & 1) ? A.p0 : A.p1;
+    const bool first = (it == 0);
+    const V vb = (V)A.sc->beta;
+    gemv_rows(A.k, A.W, [&](int c) { return A.w[c]; },
+              [&](int c, double s) {
+                  const int i = A.piv[c];
+                  const V zc = (V)s;
+                  pn[i] = first ? zc : fma_t(vb, p[i], zc);
+              },
+              s_vec);
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < A.m; i += (long long)gridDim.x * blockDim.x) {
+        if (A.pivpos[i] < 0) {
+            const V zi = A.z[i];
+            pn[i] = first ? zi : fma_t(vb, p[i], zi);
+        }
+    }
+}
+
+// ---- A: t = B^T p_new
+template <class V>
+__global__ void __launch_bounds__(kCgThreads) k_a(const CgArgs<V> A) {
+    if (cg_done(A.sc) || A.precond_only) return;
+    __shared__ double red[kCgThreads];
+    const V* pn = (A.sc->it & 1) ? A.p0 : A.p1;
+    spmv_rows<V>(A.csc, [&](int i) { return pn[i]; }, [&](int j, V s) { A.t[j] = s; }, red);
+}
+
+// ---- B: q = B t + delta p_new, partial p.q; last block: alpha
+template <class V>
+__global__ void __launch_bounds__(kCgThreads) k_b(const CgArgs<V> A) {
+    if (cg_done(A.sc) || A.precond_only) return;
+    __shared__ double red[kCgThreads];
+    const V* pn = (A.sc->it & 1) ? A.p0 : A.p1;
+    const V vd = (V)A.delta;
+    const bool has_delta = (A.delta != 0.0);
+    double pq = 0.0;
+    spmv_rows<V>(
+        A.csr, [&](int j) { return A.t[j]; },
+        [&](int i, V s) {
+            const V pi = pn[i];
+            const V qi = has_delta ? fma_t(vd, pi, s) : s;
+            A.q[i] = qi;
+            pq = fma((double)pi, (double)qi, pq);
+        },
+        red);
+    pq = block_sum(pq, red);
+    if (publish_partial(pq, A.part_pq, &A.sc->ticket[2])) {
+        const double tot = sum_parts(A.part_pq, nullptr, gridDim.x, red);
+        if (threadIdx.x == 0) {
+            CgScalars* sc = A.sc;
+            sc->ticket[2] = 0;
+            if (!(tot > 0.0)) {  // G not positive on p (breakdown) or NaN
+                sc->status = kStatusNumeric;
+                sc->done = 3;
+            } else {
+                sc->alpha = sc->rz / tot;
+                sc->rz_old = sc->rz;
+            }
+        }
+    }
+}
+
+// ---- C: x += alpha p, r_new = r - alpha q, r.r, a = W r_new_P; last block: stop?
+template <class V>
+__global__ void __launch_bounds__(kCgThreads) k_c(const CgArgs<V> A) {
+    if (cg_done(A.sc) || A.precond_only) return;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    double* s_vec = reinterpret_cast<double*>(smem_raw);
+    __shared__ double red[kCgThreads];
+    const long long it = A.sc->it;
+    const V* r = (it & 1) ? A.r1 : A.r0;
+    V* rn = (it & 1) ? A.r0 : A.r1;
+    const V* pn = (it & 1) ? A.p0 : A.p1;
+    const V va = (V)A.sc->alpha;
+    double rr = 0.0;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < A.m; i += (long long)gridDim.x * blockDim.x) {
+        const V pi = pn[i], qi = A.q[i];
+        A.x[i] = fma_t(va, pi, A.x[i]);
+        const V ri = fma_t(-va, qi, r[i]);
+        rn[i] = ri;
+        rr = fma((double)ri, (double)ri, rr);
+    }
+    rr = block_sum(rr, red);
+    gemv_rows(A.k, A.W,
+              [&](int c) {
+                  const int i = A.piv[c];
+                  return (double)fma_t(-va, A.q[i], r[i]);
+              },
+              [&](int c, double s) { A.a[c] = s; }, s_vec);
+    if (publish_partial(rr, A.part_rr, &A.sc->ticket[3])) {
+        const double tot = sum_parts(A.part_rr, nullptr, gridDim.x, red);
+        if (threadIdx.x == 0) {
+            CgScalars* sc = A.sc;
+            sc->ticket[3] = 0;
+            sc->rr = tot;
+            sc->it = it + 1;  // buffers flip for the next iteration
+            if (!(tot == tot)) {
+                sc->status = kStatusNumeric;
+                sc->done = 3;
+            } else if (tot < sc->term2 || tot == 0.0) {
+                sc->done = 1;
+            } else if (sc->it >= sc->max_iter) {
+                sc->done = 2;
+            }
+        }
     }
 }
 
 template <class V>
-cudaError_t pcg_configure(int threads, size_t smem, int* blocks_per_sm) {
-    cudaError_t e = cudaFuncSetAttribute(pcg_persistent<V>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, pcg_persistent<V>, threads, smem);
+size_t gemv_smem(const CgArgs<V>& A) {
+    return (size_t)(A.k > 0 ? A.k : 1) * sizeof(double);
+}
+
+}  // namespace
+
+template <class V>
+cudaError_t cg_configure(int k_max) {
+    const int smem = (k_max > 0 ? k_max : 1) * (int)sizeof(double);
+    cudaError_t e = cudaFuncSetAttribute(k_init<V>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_p4<V>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_c<V>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    return e;
 }
 
 template <class V>
-cudaError_t pcg_launch(const PcgArgs<V>& args, int blocks, int threads, size_t smem, cudaStream_t stream) {
-    void* params[] = {(void*)&args};
-    return cudaLaunchCooperativeKernel((const void*)pcg_persistent<V>, dim3(blocks), dim3(threads), params, smem,
-                                       stream);
+cudaError_t cg_launch_init(const CgArgs<V>& A, int blocks, cudaStream_t st) {
+    k_init<V><<<blocks, kCgThreads, gemv_smem(A), st>>>(A);
+    return cudaGetLastError();
 }
 
-template cudaError_t pcg_configure<double>(int, size_t, int*);
-template cudaError_t pcg_configure<float>(int, size_t, int*);
-template cudaError_t pcg_launch<double>(const PcgArgs<double>&, int, int, size_t, cudaStream_t);
-template cudaError_t pcg_launch<float>(const PcgArgs<float>&, int, int, size_t, cudaStream_t);
+// One iteration's six kernels (captured into a graph by the caller).
+template <class V>
+cudaError_t cg_launch_iteration(const CgArgs<V>& A, int blocks, cudaStream_t st) {
+    const size_t sm = gemv_smem(A);
+    k_p2<V><<<blocks, kCgThreads, 0, st>>>(A);
+    k_p3<V><<<blocks, kCgThreads, 0, st>>>(A);
+    k_p4<V><<<blocks, kCgThreads, sm, st>>>(A);
+    k_a<V><<<blocks, kCgThreads, 0, st>>>(A);
+    k_b<V><<<blocks, kCgThreads, 0, st>>>(A);
+    k_c<V><<<blocks, kCgThreads, sm, st>>>(A);
+    return cudaGetLastError();
+}
+
+int cg_threads() { return kCgThreads; }
+
+template cudaError_t cg_configure<double>(int);
+template cudaError_t cg_configure<float>(int);
+template cudaError_t cg_launch_init<double>(const CgArgs<double>&, int, cudaStream_t);
+template cudaError_t cg_launch_init<float>(const CgArgs<float>&, int, cudaStream_t);
+template cudaError_t cg_launch_iteration<double>(const CgArgs<double>&, int, cudaStream_t);
+template cudaError_t cg_launch_iteration<float>(const CgArgs<float>&, int, cudaStream_t);
 
 }  // namespace help

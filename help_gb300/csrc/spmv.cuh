@@ -1,112 +1,129 @@
-// CSR sparse matrix-vector products over planned work items.
+// CSR sparse matrix-vector products: y_r = sum_e val[e] * x[idx[e]] per row.
 //
-// The reference's CSRMV_N / CSRMV_T (Helper.cpp:57-81) are serial loops; the
-// transpose product is a scatter.  Here both A x and A^T x are row gathers:
-// A^T lives in HBM as its own CSR (= CSC of A), so every product is
-// "for each row: sum_e val[e] * x[idx[e]]".
+// The reference's CSRMV_N / CSRMV_T (Helper.cpp:57-81) are serial loops and
+// the transpose product is a scatter.  Here A^T lives in HBM as its own CSR
+// (= CSC of A), so both A x and A^T x are row gathers with this one routine.
 //
-// Work items (planned once per matrix on the host, see items.cpp) are either
-//   * a block of consecutive rows holding at most `cap` nonzeros: all threads
-//     of the CTA stream the block's values and indices with coalesced loads
-//     and gather the matching x entries (every load independent, so many are
-//     in flight per thread), storing value and x side by side in shared
-//     memory; then each thread accumulates one row from shared memory with
-//     one fused multiply-add per nonzero (rows longer than kThreadRowMax
-//     inside the block are taken warp-per-row), or
-//   * one row longer than `cap`, which the whole CTA reduces.
-// One FMA per nonzero and no shuffle reductions for short rows matter on
-// GB300, whose FP64 rate (~2 DFMA/clk/SM) is close to the HBM rate for SpMV.
+// Rows are split by length when the matrix is planned (host, once per matrix
+// and precision; see items.cpp):
+//   * short rows (len <= short_max = 32 G): a group of G lanes per row, G a
+//     power of two chosen so each lane handles ~4-8 nonzeros, with a floor
+//     that makes one group's loads span a whole 32-byte sector (G >= 2 for
+//     FP64, >= 8 for FP32).  A warp covers 32 / G consecutive rows, so its
+//     loads sweep one contiguous span of the value and index arrays; each lane
+//     keeps one FMA accumulator and the group combines with log2(G) shuffles;
+//   * medium rows (short_max < len <= kLongRowMin): one warp per row;
+//   * long rows (len > kLongRowMin): one CTA per row.
+// Loads go through L1 (read-only path) so the neighbouring elements a group
+// reads next reuse the sectors already fetched.  All loops are grid-stride
+// over every warp / block of the launch, so the same routine serves the
+// standalone kernels and the phases of the persistent CG kernel.  One FMA per
+// nonzero and few shuffle adds matter on GB300, whose FP64 rate (~2
+// DFMA/clk/SM) is close to the HBM rate for SpMV.
 #pragma once
 
 #include "common.cuh"
 
 namespace help {
 
-constexpr int kItemHasLongRows = 1 << 30;  // flag in item.y: some row > kThreadRowMax
-constexpr int kItemRowMask = (1 << 30) - 1;
-constexpr int kThreadRowMax = 48;
-
-// Shared-memory bytes spmv_items needs for a given cap.
+// Device view of one planned CSR matrix.
 template <class V>
-constexpr size_t spmv_smem_bytes(int cap) {
-    return (size_t)cap * 2 * sizeof(V);
-}
+struct SpmvView {
+    int rows;
+    int G;          // lanes per short row (power of two, 1..32)
+    int short_max;  // rows longer than this are in med_rows or long_rows
+    int n_med, n_long;
+    const int* ptr;
+    const int* idx;
+    const V* val;
+    const int* med_rows;   // warp-per-row
+    const int* long_rows;  // CTA-per-row
+};
 
-// Process items first, first + stride, ... of the list.
-//   xf(col)       -> V      value of the dense operand at index `col`
-//   ep(row, sum)             epilogue for one finished row (called by one thread)
-// s_val / s_x: shared staging of `cap` entries each; red: blockDim/32 doubles.
+//   xf(col)  -> V     value of the dense operand at index `col`
+//   ep(row, sum)      epilogue for one finished row (called by one thread)
+// red: blockDim doubles of shared memory (CTA reductions of long rows).
 template <class V, class XF, class EP>
-HELP_DEVINL void spmv_items(const int4* __restrict__ items, int n_items, int first, int stride,
-                            const int* __restrict__ ptr, const int* __restrict__ idx,
-                            const V* __restrict__ val, int cap, const XF& xf, const EP& ep, V* s_val,
-                            V* s_x, double* red) {
+HELP_DEVINL void spmv_rows(const SpmvView<V>& M, const XF& xf, const EP& ep, double* red) {
     const int tid = threadIdx.x, nthr = blockDim.x;
-    const int lane = tid & 31, warp = tid >> 5, nwarps = nthr >> 5;
-    for (int it = first; it < n_items; it += stride) {
-        const int4 w = ld_ro(items + it);
-        const int row0 = w.x, row1 = w.y & kItemRowMask;
-        const int e0 = w.z, e1 = w.w;
-        if (e1 - e0 > cap) {
-            // one long row: strided FMA per thread, deterministic block reduction
-            V acc = V(0);
-            int e = e0 + tid;
-            for (; e + 3 * nthr < e1; e += 4 * nthr) {
-                const int c0 = ld_stream(idx + e), c1 = ld_stream(idx + e + nthr);
-                const int c2 = ld_stream(idx + e + 2 * nthr), c3 = ld_stream(idx + e + 3 * nthr);
-                const V v0 = ld_stream(val + e), v1 = ld_stream(val + e + nthr);
-                const V v2 = ld_stream(val + e + 2 * nthr), v3 = ld_stream(val + e + 3 * nthr);
-                const V x0 = xf(c0), x1 = xf(c1), x2 = xf(c2), x3 = xf(c3);
-                acc = fma_t(v0, x0, acc);
-                acc = fma_t(v1, x1, acc);
-                acc = fma_t(v2, x2, acc);
-                acc = fma_t(v3, x3, acc);
-            }
-            for (; e < e1; e += nthr) acc = fma_t(ld_stream(val + e), xf(ld_stream(idx + e)), acc);
-            const double s = block_sum((double)acc, red);
-            if (tid == 0) ep(row0, (V)s);
-            continue;
+    const int lane = tid & 31, warp = tid >> 5, nw = nthr >> 5;
+    const int gw = blockIdx.x * nw + warp, tw = gridDim.x * nw;
+    const int* __restrict__ ptr = M.ptr;
+    const int* __restrict__ idx = M.idx;
+    const V* __restrict__ val = M.val;
+
+    // long rows: the whole CTA
+    for (int i = blockIdx.x; i < M.n_long; i += gridDim.x) {
+        const int r = ld_ro(M.long_rows + i);
+        const int b = ld_ro(ptr + r), e = ld_ro(ptr + r + 1);
+        V acc = V(0);
+        int q = b + tid;
+        for (; q + 3 * nthr < e; q += 4 * nthr) {
+            const int c0 = ld_ro(idx + q), c1 = ld_ro(idx + q + nthr);
+            const int c2 = ld_ro(idx + q + 2 * nthr), c3 = ld_ro(idx + q + 3 * nthr);
+            const V v0 = ld_ro(val + q), v1 = ld_ro(val + q + nthr);
+            const V v2 = ld_ro(val + q + 2 * nthr), v3 = ld_ro(val + q + 3 * nthr);
+            const V x0 = xf(c0), x1 = xf(c1), x2 = xf(c2), x3 = xf(c3);
+            acc = fma_t(v0, x0, acc);
+            acc = fma_t(v1, x1, acc);
+            acc = fma_t(v2, x2, acc);
+            acc = fma_t(v3, x3, acc);
         }
-        const int ne = e1 - e0;
-        {
-            int e = tid;
-            for (; e + 3 * nthr < ne; e += 4 * nthr) {
-                const int c0 = ld_stream(idx + e0 + e), c1 = ld_stream(idx + e0 + e + nthr);
-                const int c2 = ld_stream(idx + e0 + e + 2 * nthr), c3 = ld_stream(idx + e0 + e + 3 * nthr);
-                const V v0 = ld_stream(val + e0 + e), v1 = ld_stream(val + e0 + e + nthr);
-                const V v2 = ld_stream(val + e0 + e + 2 * nthr), v3 = ld_stream(val + e0 + e + 3 * nthr);
-                const V x0 = xf(c0), x1 = xf(c1), x2 = xf(c2), x3 = xf(c3);
-                s_val[e] = v0, s_val[e + nthr] = v1, s_val[e + 2 * nthr] = v2, s_val[e + 3 * nthr] = v3;
-                s_x[e] = x0, s_x[e + nthr] = x1, s_x[e + 2 * nthr] = x2, s_x[e + 3 * nthr] = x3;
-            }
-            for (; e < ne; e += nthr) {
-                const int c = ld_stream(idx + e0 + e);
-                s_val[e] = ld_stream(val + e0 + e);
-                s_x[e] = xf(c);
-            }
+        for (; q < e; q += nthr) acc = fma_t(ld_ro(val + q), xf(ld_ro(idx + q)), acc);
+        const double s = block_sum((double)acc, red);
+        if (tid == 0) ep(r, (V)s);
+    }
+
+    // medium rows: one warp each
+    for (int i = gw; i < M.n_med; i += tw) {
+        const int r = ld_ro(M.med_rows + i);
+        const int b = ld_ro(ptr + r), e = ld_ro(ptr + r + 1);
+        V acc = V(0);
+        int q = b + lane;
+        for (; q + 96 < e; q += 128) {
+            const int c0 = ld_ro(idx + q), c1 = ld_ro(idx + q + 32);
+            const int c2 = ld_ro(idx + q + 64), c3 = ld_ro(idx + q + 96);
+            const V v0 = ld_ro(val + q), v1 = ld_ro(val + q + 32);
+            const V v2 = ld_ro(val + q + 64), v3 = ld_ro(val + q + 96);
+            const V x0 = xf(c0), x1 = xf(c1), x2 = xf(c2), x3 = xf(c3);
+            acc = fma_t(v0, x0, acc);
+            acc = fma_t(v1, x1, acc);
+            acc = fma_t(v2, x2, acc);
+            acc = fma_t(v3, x3, acc);
         }
-        __syncthreads();
-        const int nr = row1 - row0;
-        for (int r = tid; r < nr; r += nthr) {
-            const int b = ld_ro(ptr + row0 + r) - e0, e = ld_ro(ptr + row0 + r + 1) - e0;
-            if (e - b <= kThreadRowMax) {
-                V acc = V(0);
-                for (int q = b; q < e; ++q) acc = fma_t(s_val[q], s_x[q], acc);
-                ep(row0 + r, acc);
-            }
+        for (; q < e; q += 32) acc = fma_t(ld_ro(val + q), xf(ld_ro(idx + q)), acc);
+        acc = warp_sum(acc);
+        if (lane == 0) ep(r, acc);
+    }
+
+    // short rows: G lanes per row, 32 / G rows per warp step
+    const int G = M.G, lg = __ffs(G) - 1;
+    const int sub = lane & (G - 1), rpw = 32 >> lg;
+    for (int base = gw * rpw; base < M.rows; base += tw * rpw) {
+        const int r = base + (lane >> lg);
+        int b = 0, e = 0;
+        if (r < M.rows) {
+            b = ld_ro(ptr + r);
+            e = ld_ro(ptr + r + 1);
         }
-        if (w.y & kItemHasLongRows) {
-            for (int r = warp; r < nr; r += nwarps) {
-                const int b = ld_ro(ptr + row0 + r) - e0, e = ld_ro(ptr + row0 + r + 1) - e0;
-                if (e - b > kThreadRowMax) {
-                    V acc = V(0);
-                    for (int q = b + lane; q < e; q += 32) acc = fma_t(s_val[q], s_x[q], acc);
-                    acc = warp_sum(acc);
-                    if (lane == 0) ep(row0 + r, acc);
-                }
-            }
+        const bool mine = (r < M.rows) && (e - b <= M.short_max);
+        if (!mine) e = b;
+        V acc = V(0);
+        int q = b + sub;
+        for (; q + 3 * G < e; q += 4 * G) {
+            const int c0 = ld_ro(idx + q), c1 = ld_ro(idx + q + G);
+            const int c2 = ld_ro(idx + q + 2 * G), c3 = ld_ro(idx + q + 3 * G);
+            const V v0 = ld_ro(val + q), v1 = ld_ro(val + q + G);
+            const V v2 = ld_ro(val + q + 2 * G), v3 = ld_ro(val + q + 3 * G);
+            const V x0 = xf(c0), x1 = xf(c1), x2 = xf(c2), x3 = xf(c3);
+            acc = fma_t(v0, x0, acc);
+            acc = fma_t(v1, x1, acc);
+            acc = fma_t(v2, x2, acc);
+            acc = fma_t(v3, x3, acc);
         }
-        __syncthreads();
+        for (; q < e; q += G) acc = fma_t(ld_ro(val + q), xf(ld_ro(idx + q)), acc);
+        for (int o = G >> 1; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+        if (mine && sub == 0) ep(r, acc);
     }
 }
 

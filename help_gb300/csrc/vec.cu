@@ -11,16 +11,12 @@ namespace help {
 namespace {
 
 template <class V, int EPI>
-__global__ void __launch_bounds__(512) k_spmv(const int4* __restrict__ items, int n_items, const int* __restrict__ ptr,
-                                              const int* __restrict__ idx, const V* __restrict__ val, int cap,
-                                              const V* __restrict__ x, V* __restrict__ y, const V* __restrict__ aux,
-                                              const V* __restrict__ aux2, const double* __restrict__ s2, double delta) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    V* s_val = reinterpret_cast<V*>(smem_raw);
-    V* s_x = s_val + cap;
-    __shared__ double red[32];
-    spmv_items<V>(
-        items, n_items, blockIdx.x, gridDim.x, ptr, idx, val, cap, [&](int c) { return ld_ro(x + c); },
+__global__ void __launch_bounds__(256) k_spmv(const SpmvView<V> M, const V* __restrict__ x, V* __restrict__ y,
+                                              const V* __restrict__ aux, const V* __restrict__ aux2,
+                                              const double* __restrict__ s2, double delta) {
+    __shared__ double red[256];
+    spmv_rows<V>(
+        M, [&](int c) { return ld_ro(x + c); },
         [&](int row, V s) {
             if (EPI == kEpiStore) {
                 y[row] = s;
@@ -34,7 +30,7 @@ __global__ void __launch_bounds__(512) k_spmv(const int4* __restrict__ items, in
                 y[row] = fma_t((V)delta, aux[row], s);
             }
         },
-        s_val, s_x, red);
+        red);
 }
 
 __global__ void k_mul(const double* __restrict__ a, const double* __restrict__ b, double* __restrict__ out, int64_t n) {
@@ -66,7 +62,7 @@ __global__ void k_fill_f32(float* __restrict__ x, float v, int64_t n) {
         x[i] = v;
 }
 __global__ void k_sumsq_part(const double* __restrict__ x, int64_t n, double* __restrict__ part) {
-    __shared__ double red[32];
+    __shared__ double red[1024];
     double s = 0.0;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
         s = fma(x[i], x[i], s);
@@ -74,7 +70,7 @@ __global__ void k_sumsq_part(const double* __restrict__ x, int64_t n, double* __
     if (threadIdx.x == 0) part[blockIdx.x] = s;
 }
 __global__ void k_sum_parts(const double* __restrict__ part, int np, double* __restrict__ out) {
-    __shared__ double red[32];
+    __shared__ double red[1024];
     double s = 0.0;
     for (int i = threadIdx.x; i < np; i += blockDim.x) s += part[i];
     s = block_sum(s, red);
@@ -90,39 +86,34 @@ inline int grid_for(int64_t n, int threads) {
 
 }  // namespace
 
-template <class V>
-cudaError_t spmv_launch(int epi, const int4* items, int n_items, const int* ptr, const int* idx, const V* val, int cap,
-                        const V* x, V* y, const V* aux, const V* aux2, const double* s2, double delta, int blocks,
-                        int threads, cudaStream_t stream) {
-    if (n_items <= 0) return cudaSuccess;
-    const size_t smem = spmv_smem_bytes<V>(cap);
-    if (blocks <= 0 || blocks > n_items) blocks = n_items;
-    cudaError_t e = cudaSuccess;
-#define HELP_SPMV_CASE(E)                                                                                     \
-    case E:                                                                                                   \
-        e = cudaFuncSetAttribute(k_spmv<V, E>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);       \
-        if (e != cudaSuccess) return e;                                                                       \
-        k_spmv<V, E><<<blocks, threads, smem, stream>>>(items, n_items, ptr, idx, val, cap, x, y, aux, aux2, s2, delta); \
-        break;
-    switch (epi) {
-        HELP_SPMV_CASE(kEpiStore)
-        HELP_SPMV_CASE(kEpiRhs)
-        HELP_SPMV_CASE(kEpiBacksub)
-        HELP_SPMV_CASE(kEpiResid)
-        HELP_SPMV_CASE(kEpiAddDelta)
-        default:
-            return cudaErrorInvalidValue;
-    }
-#undef HELP_SPMV_CASE
+template <class V, int E>
+cudaError_t spmv_launch_one(const SpmvView<V>& M, const V* x, V* y, const V* aux, const V* aux2, const double* s2,
+                            double delta, int blocks, int threads, cudaStream_t stream) {
+    k_spmv<V, E><<<blocks, threads, 0, stream>>>(M, x, y, aux, aux2, s2, delta);
     return cudaGetLastError();
 }
 
-template cudaError_t spmv_launch<double>(int, const int4*, int, const int*, const int*, const double*, int,
-                                         const double*, double*, const double*, const double*, const double*, double,
-                                         int, int, cudaStream_t);
-template cudaError_t spmv_launch<float>(int, const int4*, int, const int*, const int*, const float*, int, const float*,
-                                        float*, const float*, const float*, const double*, double, int, int,
-                                        cudaStream_t);
+template <class V>
+cudaError_t spmv_launch(int epi, const SpmvView<V>& M, const V* x, V* y, const V* aux, const V* aux2,
+                        const double* s2, double delta, int blocks, int threads, cudaStream_t stream) {
+    if (M.rows <= 0) return cudaSuccess;
+    if (blocks <= 0) blocks = 1;
+    switch (epi) {
+        case kEpiStore: return spmv_launch_one<V, kEpiStore>(M, x, y, aux, aux2, s2, delta, blocks, threads, stream);
+        case kEpiRhs: return spmv_launch_one<V, kEpiRhs>(M, x, y, aux, aux2, s2, delta, blocks, threads, stream);
+        case kEpiBacksub: return spmv_launch_one<V, kEpiBacksub>(M, x, y, aux, aux2, s2, delta, blocks, threads, stream);
+        case kEpiResid: return spmv_launch_one<V, kEpiResid>(M, x, y, aux, aux2, s2, delta, blocks, threads, stream);
+        case kEpiAddDelta:
+            return spmv_launch_one<V, kEpiAddDelta>(M, x, y, aux, aux2, s2, delta, blocks, threads, stream);
+        default:
+            return cudaErrorInvalidValue;
+    }
+}
+
+template cudaError_t spmv_launch<double>(int, const SpmvView<double>&, const double*, double*, const double*,
+                                         const double*, const double*, double, int, int, cudaStream_t);
+template cudaError_t spmv_launch<float>(int, const SpmvView<float>&, const float*, float*, const float*, const float*,
+                                        const double*, double, int, int, cudaStream_t);
 
 cudaError_t vec_scale_mul(const double* a, const double* b, double* out, int64_t n, cudaStream_t st) {
     k_mul<<<grid_for(n, 256), 256, 0, st>>>(a, b, out, n);

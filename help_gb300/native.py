@@ -25,6 +25,8 @@ HELP_PREC_MIXED = 1
 HELP_OP_A = 0
 HELP_OP_AT = 1
 HELP_OP_ADAT = 2
+HELP_OP_B = 3
+HELP_OP_BT = 4
 
 # ---- instance families (help_lp.h)
 HELP_LP_RANDOM = 0
@@ -69,6 +71,11 @@ class PcgStats(C.Structure):
         ("nnz_c", C.c_int64),
         ("solves", C.c_int32),
         ("renews", C.c_int32),
+        ("cg_kernel_ms", C.c_double),
+        ("cg_kernel_ms_total", C.c_double),
+        ("cg_iterations_fp32", C.c_int64),
+        ("cg_launches", C.c_int32),
+        ("dense_regularised", C.c_int32),
     ]
 
 

@@ -74,6 +74,12 @@ typedef struct help_pcg_stats {
     double renew_ms, solve_ms;   /* last renew / solve wall time                       */
     int64_t nnz_c;               /* entries of the pivot-column block G[:,P] (non-pivot rows) */
     int32_t solves, renews;
+    /* device time of the persistent CG kernel (CUDA events on the launching stream) */
+    double cg_kernel_ms;         /* last solve, all CG launches                        */
+    double cg_kernel_ms_total;   /* since construct                                    */
+    int64_t cg_iterations_fp32;  /* last solve: iterations run in FP32 (mixed)          */
+    int32_t cg_launches;         /* last solve                                          */
+    int32_t dense_regularised;   /* last renew: pivots raised to the floor in G11       */
 } help_pcg_stats;
 
 /* Fills *opt with the defaults (FP64, k = 10, cg_tol = 1e-20 as the reference). */
@@ -113,10 +119,12 @@ const char* help_pcg_last_error(const help_pcg* ctx);
 /* ---- building blocks of the path, exposed for parity tests and the isolated
  * ADA^T v benchmark.  Host arrays unless the name ends in _dev. ---- */
 
-enum { HELP_OP_A = 0, HELP_OP_AT = 1, HELP_OP_ADAT = 2 };
+enum { HELP_OP_A = 0, HELP_OP_AT = 1, HELP_OP_ADAT = 2, HELP_OP_B = 3, HELP_OP_BT = 4 };
 
 /* y = A x (CSRMV_N, Helper.cpp:57-68), y = A^T x (CSRMV_T, Helper.cpp:71-81)
- * or y = (A D^-1 A^T + delta I) x (PCG.cpp:346-358), D from the last renew. */
+ * or y = (A D^-1 A^T + delta I) x (PCG.cpp:346-358), D from the last renew.
+ * HELP_OP_B / HELP_OP_BT are the two passes of the last one, with
+ * B = A D^-1/2: y = B x (x has n entries) and y = B^T x (x has m entries). */
 int help_pcg_matvec(help_pcg* ctx, int32_t op, const double* x, double* y);
 /* Same on device pointers, on `stream` (a cudaStream_t, NULL = default);
  * fp32 != 0 runs the FP32 copy of B (x, y are then float*). */
