@@ -52,7 +52,7 @@ struct RowPlan {
 constexpr int kGminF64 = 2;  // 2 lanes x 8 B = a 16-byte run per load, sector reuse through L1
 constexpr int kGminF32 = 8;  // 8 lanes x 4 B = one 32-byte sector per load
 
-// Results the persistent CG kernel leaves behind.
+// Results a CG run leaves behind.
 struct CgOut {
     long long iterations;
     double rr0;

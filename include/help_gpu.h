@@ -60,7 +60,7 @@ typedef struct help_pcg_options {
     /* warm start / learned correction */
     int32_t warm_start;      /* 1: start CG from the previous solve's x_2 of this renew */
     int32_t fallback;        /* 1: on cap or failed FP64 check, redo with plain FP64 PCG */
-    int32_t threads;         /* persistent-kernel block size (0 = default)              */
+    int32_t threads;         /* reserved (ignored; kernels size their own blocks)       */
 } help_pcg_options;
 
 typedef struct help_pcg_stats {
@@ -74,7 +74,7 @@ typedef struct help_pcg_stats {
     double renew_ms, solve_ms;   /* last renew / solve wall time                       */
     int64_t nnz_c;               /* entries of the pivot-column block G[:,P] (non-pivot rows) */
     int32_t solves, renews;
-    /* device time of the persistent CG kernel (CUDA events on the launching stream) */
+    /* device time of the CG graph launches (CUDA events on the launching stream) */
     double cg_kernel_ms;         /* last solve, all CG launches                        */
     double cg_kernel_ms_total;   /* since construct                                    */
     int64_t cg_iterations_fp32;  /* last solve: iterations run in FP32 (mixed)          */

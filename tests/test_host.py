@@ -101,6 +101,25 @@ def test_lp_library_exports_every_declared_symbol():
         getattr(lib, s)
 
 
+@pytest.mark.skipif(not ob.ref_available(), reason="the reference's sources were not built here")
+def test_reference_program_links_against_gpu_backend():
+    """The reference program (every source but UsePCG_CPU.cpp + PCG.cpp) links
+    with help_gb300/csrc/UsePCG_GPU.cpp over libhelp_gpu.so: all four LP.h
+    entry points resolve to the shim and nothing is left undefined."""
+    import subprocess
+    r = subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle", "ref"), "../_ref/help_ref_gpu"],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
+    exe = os.path.join(ROOT, "oracle", "_ref", "help_ref_gpu")
+    syms = subprocess.run(["nm", "-C", exe], capture_output=True, text=True).stdout
+    for f in ("LinearEquation_Construct()", "LinearEquation_Destruct()", "RenewLinearEquation(double*)",
+              "SolveLinearEquation(double*, double*, double*, double*, double*)"):
+        assert re.search(r" T " + re.escape(f), syms), f
+    assert "ConjugateGradient" not in syms  # the reference's CPU PCG is not linked in
+    dyn = subprocess.run(["nm", "-D", "--undefined-only", exe], capture_output=True, text=True).stdout
+    assert "help_pcg_solve" in dyn
+
+
 def test_hsd_driver_objective_matches_scipy():
     scipy_opt = pytest.importorskip("scipy.optimize")
     import scipy.sparse as sp
