@@ -167,7 +167,7 @@ GPU_SYMBOLS = [
     "help_pcg_default_options", "help_pcg_create", "help_pcg_free", "help_pcg_construct",
     "help_pcg_renew", "help_pcg_solve", "help_pcg_destruct", "help_pcg_get_stats",
     "help_pcg_last_error", "help_pcg_matvec", "help_pcg_matvec_dev", "help_pcg_precond_apply",
-    "help_pcg_get_pivots", "help_pcg_cg", "help_adat_assemble",
+    "help_pcg_get_pivots", "help_pcg_cg", "help_adat_assemble", "help_adat_matvec_noalloc",
 ]
 LP_SYMBOLS = [
     "help_lp_generate", "help_lp_free", "help_lp_write_mps", "help_csc_to_csr",
@@ -210,6 +210,7 @@ def gpu_lib() -> C.CDLL:
         lib.help_pcg_get_pivots.argtypes = [vp, dp, dp, dp]
         lib.help_pcg_cg.argtypes = [vp, dp, dp, C.POINTER(C.c_int64)]
         lib.help_adat_assemble.argtypes = [vp, dp, dp, dp, dp, C.POINTER(C.c_int64)]
+        lib.help_adat_matvec_noalloc.argtypes = [i32, i32, i64] + [vp] * 10
         for s in GPU_SYMBOLS:
             getattr(lib, s)
         _gpu = lib

@@ -147,6 +147,32 @@ int help_pcg_cg(help_pcg* ctx, const double* b, double* x, int64_t* iters);
 int help_adat_assemble(help_pcg* ctx, const double* w, int32_t* row_ptr, int32_t* col, double* val,
                        int64_t* nnz);
 
+/* ---- no-allocation product (no counterpart in the reference) ----
+ *
+ * y = A D^-1 A^T x for callers that cannot allocate device memory (code
+ * running under another runtime's memory pool or an allocator that forbids
+ * new allocations, paths that must not allocate after start-up, hosts that
+ * only receive device pointers).  Everything is the caller's device memory --
+ * A as CSR (row_ptr[m+1], col_ind[nnz], val[nnz]) and as CSC
+ * (col_ptr[n+1], row_ind[nnz], val_t[nnz]), d[n], x[m], y[m] -- except the
+ * intermediate D^-1 A^T x, which lives in a fixed device array of 2^20
+ * doubles (8 MiB) that every GPU loading the library keeps until the process
+ * exits.  No cudaMalloc, cudaFree or allocating library call is made.
+ *   - n larger than 2^20 is rejected with HELP_E_ARG;
+ *   - the first call on a device looks up that array's device address (once
+ *     per device, that device current): make the first call before any
+ *     stream capture;
+ *   - every call on a device shares the array, so calls that overlap on the
+ *     GPU (other streams, other host threads) race: serialise them;
+ *   - nothing has to start at zero: the first pass writes every entry of the
+ *     array that the second pass reads, and y is written in full;
+ *   - runs on `stream` (NULL = the legacy default stream) on the current device.
+ */
+int help_adat_matvec_noalloc(int32_t m, int32_t n, int64_t nnz, const int32_t* row_ptr,
+                             const int32_t* col_ind, const double* val, const int32_t* col_ptr,
+                             const int32_t* row_ind, const double* val_t, const double* d,
+                             const double* x, double* y, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
