@@ -48,7 +48,7 @@ class GpuNormalEquations:
     def __init__(self, pivots: int = 10, precision: str = "fp64", cg_tol: float = 1e-20,
                  cg_max_iter: int = 1_000_000, delta: float = 0.0, ir_tol: float = 1e-10,
                  ir_max_outer: int = 10, inner_tol: float = 1e-5, inner_max_iter: int = 200_000,
-                 warm_start: bool = False, fallback: bool = True, device: int = 0, threads: int = 0):
+                 warm_start: bool = False, fallback: bool = True, device: int = 0, cg_path: str = "auto"):
         self.lib = native.gpu_lib()
         o = native.PcgOptions()
         self.lib.help_pcg_default_options(C.byref(o))
@@ -64,7 +64,7 @@ class GpuNormalEquations:
         o.inner_max_iter = int(inner_max_iter)
         o.warm_start = int(bool(warm_start))
         o.fallback = int(bool(fallback))
-        o.threads = threads
+        o.cg_path = {"auto": 0, "graph": 1, "cluster": 2}[cg_path]
         self.options = o
         h = C.c_void_p()
         self._check(self.lib.help_pcg_create(C.byref(o), C.byref(h)), None)

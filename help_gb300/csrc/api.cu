@@ -15,11 +15,16 @@
 #include <vector>
 
 #include "context.h"
+#include "mlp.h"
 #include "items.h"
 #include "kernels.h"
 #include "spmv.cuh"
 
 using namespace help;
+
+// model internals for the solver (mlp_api.cu)
+const help::MlpDevWeights* help_mlp_device_weights(const help_mlp* mlp);
+int help_mlp_device(const help_mlp* mlp);
 
 namespace {
 
@@ -137,6 +142,29 @@ struct CgResult {
     int status = 0;
 };
 
+// FP64-equivalent work of one CG iteration: below kClusterWorkMax one
+// thread-block cluster runs the iterations faster than six launches per
+// iteration over the whole GPU.
+int64_t cluster_work(const help_pcg* ctx) {
+    return 2 * (ctx->nnz + ctx->nnz_c) + 8 * (int64_t)ctx->m + (int64_t)ctx->k * ctx->k;
+}
+
+int finish_pcg(help_pcg* ctx, bool f32, const CgScalars* h, CgResult* res) {
+    CK(cudaEventSynchronize(ctx->ev1));
+    float kms = 0.f;
+    CK(cudaEventElapsedTime(&kms, ctx->ev0, ctx->ev1));
+    ctx->solve_kernel_ms += kms;
+    ctx->solve_launches += 1;
+    if (f32) ctx->solve_iters_f32 += h->it;
+    res->iterations = h->it;
+    res->rr0 = h->rr0;
+    res->rr = h->rr;
+    res->converged = (h->done == 1);
+    res->status = h->status;
+    if (h->done == 3) return fail(ctx, HELP_E_NUMERIC, "pcg: breakdown (non-positive curvature or NaN)");
+    return HELP_OK;
+}
+
 template <class V>
 int run_pcg(help_pcg* ctx, V* x, V* r0, double tol, long long max_iter, int precond_only, CgResult* res) {
     const bool f32 = std::is_same<V, float>::value;
@@ -180,6 +208,27 @@ int run_pcg(help_pcg* ctx, V* x, V* r0, double tol, long long max_iter, int prec
     h->tol2 = tol * tol;
     h->max_iter = max_iter;
     CK(cudaMemcpyAsync(&c->cg, h, sizeof(CgScalars), cudaMemcpyHostToDevice, ctx->stream));
+    const int cs = ctx->cluster_cs[slot];
+    bool cluster = false;
+    if (!precond_only && cs > 0) {
+        if (ctx->opt.cg_path == 2) cluster = true;
+        else if (ctx->opt.cg_path == 0) cluster = cluster_work(ctx) <= kClusterWorkMax;
+    }
+    ctx->stats.cg_path_used = cluster ? 2 : 1;
+    if (cluster) {
+        CK(cudaEventRecord(ctx->ev0, ctx->stream));
+        CK(cg_launch_init<V>(A, nb, ctx->stream));
+        int per = 64;
+        for (;;) {
+            CK(cg_launch_cluster<V>(A, cs, per, ctx->stream));
+            CK(cudaMemcpyAsync(h, &c->cg, sizeof(CgScalars), cudaMemcpyDeviceToHost, ctx->stream));
+            CK(cudaStreamSynchronize(ctx->stream));
+            if (h->done != 0) break;
+            per = std::min(per * 2, 4096);
+        }
+        CK(cudaEventRecord(ctx->ev1, ctx->stream));
+        return finish_pcg(ctx, f32, h, res);
+    }
     // (re)capture the per-iteration graph when the arguments changed
     std::vector<unsigned char>& key = ctx->graph_args[slot];
     if (!ctx->graph_exec[slot] || key.size() != sizeof(A) || std::memcmp(key.data(), &A, sizeof(A)) != 0) {
@@ -208,19 +257,7 @@ int run_pcg(help_pcg* ctx, V* x, V* r0, double tol, long long max_iter, int prec
         if (h->done != 0 || precond_only) break;
     }
     CK(cudaEventRecord(ctx->ev1, ctx->stream));
-    CK(cudaEventSynchronize(ctx->ev1));
-    float kms = 0.f;
-    CK(cudaEventElapsedTime(&kms, ctx->ev0, ctx->ev1));
-    ctx->solve_kernel_ms += kms;
-    ctx->solve_launches += 1;
-    if (f32) ctx->solve_iters_f32 += h->it;
-    res->iterations = h->it;
-    res->rr0 = h->rr0;
-    res->rr = h->rr;
-    res->converged = (h->done == 1);
-    res->status = h->status;
-    if (h->done == 3) return fail(ctx, HELP_E_NUMERIC, "pcg: breakdown (non-positive curvature or NaN)");
-    return HELP_OK;
+    return finish_pcg(ctx, f32, h, res);
 }
 
 // res = rhs - G x  (FP64), returns ||res||^2 in *rr (host)
@@ -278,6 +315,8 @@ int normal_solve(help_pcg* ctx, const double* rhs, double* x, bool warm, long lo
         return HELP_OK;
     }
     // Mixed precision: FP32 CG corrections inside FP64 iterative refinement.
+    // Once FP32 corrections stagnated (the interior-point iterates only get
+    // worse conditioned), later solves go straight to FP64 PCG.
     if (!warm) CK(vec_fill(x, 0.0, m, ctx->stream));
     double rr = 0.0;
     rc = residual_f64(ctx, x, rhs, r, &rr);
@@ -286,7 +325,7 @@ int normal_solve(help_pcg* ctx, const double* rhs, double* x, bool warm, long lo
     int outer = 0;
     bool ok = (rr <= target2) || rhs2 == 0.0;
     double prev = rr;
-    while (!ok && outer < ctx->opt.ir_max_outer) {
+    while (!ok && !ctx->fp32_stagnated && outer < ctx->opt.ir_max_outer) {
         // scale the residual to unit norm before narrowing to FP32
         const double scale = std::sqrt(rr);
         CK(vec_to_f32_scaled(r, 1.0 / scale, ctx->r032.as<float>(), m, ctx->stream));
@@ -301,7 +340,10 @@ int normal_solve(help_pcg* ctx, const double* rhs, double* x, bool warm, long lo
         if (rc) return rc;
         ++outer;
         ok = (rr <= target2);
-        if (!ok && !(rr < 0.25 * prev)) break;  // stagnation: FP32 corrections no longer help
+        if (!ok && !(rr < 0.25 * prev)) {  // stagnation: FP32 corrections no longer help
+            ctx->fp32_stagnated = true;
+            break;
+        }
         prev = rr;
     }
     *outer_out = outer;
@@ -397,6 +439,76 @@ void release_all(help_pcg* ctx) {
 int read_int(help_pcg* ctx, const int* dev, int* out) {
     CK(cudaMemcpyAsync(out, dev, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
+    return HELP_OK;
+}
+
+// Features of the current renew into X (BF16 [m][16]) with the attached
+// model's normalisation.
+int learned_features(help_pcg* ctx, __nv_bfloat16* X, float* R) {
+    const int prev = ctx->x2_cur ^ 1;
+    const double* xprev = ctx->x2_have[prev][0] ? ctx->x2h[prev][0].as<double>() : nullptr;
+    double* part = ctx->partials.as<double>() + 4096;
+    if (xprev) CK(vec_sumsq(xprev, ctx->m, part, part + 2048, ctx->stream));
+    CK(mlp_features(ctx->rp.as<int>(), ctx->ci.as<int>(), ctx->d.as<double>(), ctx->diag.as<double>(),
+                    ctx->dsinv.as<double>(), ctx->pivpos.as<int>(), xprev, part + 2048, ctx->m,
+                    ctx->mlp ? help_mlp_device_weights(ctx->mlp) : nullptr, X, R, ctx->stream));
+    return HELP_OK;
+}
+
+// After a renew with a model attached: features, forward, corrected D_S^-1
+// (the plain one kept for the fallback).
+int learned_renew(help_pcg* ctx) {
+    const int m = ctx->m;
+    CK(ctx->mlp_x.ensure(2 * (size_t)HELP_MLP_IN * m));
+    CK(ctx->mlp_out.ensure(sizeof(float) * HELP_MLP_OUT * (size_t)m));
+    CK(ctx->dsinv_plain.ensure(8 * (size_t)m));
+    int rc = learned_features(ctx, ctx->mlp_x.as<__nv_bfloat16>(), nullptr);
+    if (rc) return rc;
+    CK(mlp_forward(ctx->mlp_x.as<__nv_bfloat16>(), m, help_mlp_device_weights(ctx->mlp), ctx->mlp_out.as<float>(),
+                   nullptr, nullptr, ctx->num_sms, ctx->stream));
+    CK(cudaMemcpyAsync(ctx->dsinv_plain.p, ctx->dsinv.p, 8 * (size_t)m, cudaMemcpyDeviceToDevice, ctx->stream));
+    const bool mixed = ctx->opt.precision == HELP_PREC_MIXED;
+    CK(mlp_apply_diag(ctx->mlp_out.as<float>(), ctx->pivpos.as<int>(), ctx->dsinv.as<double>(),
+                      mixed ? ctx->dsinv32.as<float>() : nullptr, m, ctx->stream));
+    ctx->mlp_active = true;
+    return HELP_OK;
+}
+
+// Undo the model's correction for the rest of this renew.
+int learned_restore(help_pcg* ctx) {
+    const int m = ctx->m;
+    CK(cudaMemcpyAsync(ctx->dsinv.p, ctx->dsinv_plain.p, 8 * (size_t)m, cudaMemcpyDeviceToDevice, ctx->stream));
+    if (ctx->opt.precision == HELP_PREC_MIXED)
+        CK(vals_to_f32(ctx->dsinv.as<double>(), ctx->dsinv32.as<float>(), m, ctx->stream));
+    ctx->mlp_active = false;
+    return HELP_OK;
+}
+
+// x = alpha v, v = out[:,1] .* x_2 of this slot in the previous renew, alpha
+// minimising the G-norm error along v.  *used = false when there is no
+// previous solution or v is zero.
+int learned_warm_start(help_pcg* ctx, int slot, bool* used) {
+    *used = false;
+    const int prev = ctx->x2_cur ^ 1;
+    if (!ctx->x2_have[prev][slot]) return HELP_OK;
+    const int m = ctx->m;
+    double* x = ctx->x.as<double>();
+    double* gv = ctx->res.as<double>();
+    CK(mlp_warm_vector(ctx->mlp_out.as<float>(), ctx->x2h[prev][slot].as<double>(), x, m, ctx->stream));
+    CK(spmv_launch<double>(kEpiStore, view<double>(ctx->pl_csc, ctx->cp, ctx->ri, ctx->bvT), x, ctx->t.as<double>(),
+                           nullptr, nullptr, nullptr, 0.0, spmv_blocks(ctx), kSpmvThreads, ctx->stream));
+    CK(spmv_launch<double>(kEpiAddDelta, view<double>(ctx->pl_csr, ctx->rp, ctx->ci, ctx->bv), ctx->t.as<double>(), gv,
+                           x, nullptr, nullptr, ctx->opt.delta, spmv_blocks(ctx), kSpmvThreads, ctx->stream));
+    double* part = ctx->partials.as<double>() + 4096;
+    CK(vec_dot(x, ctx->rhs.as<double>(), m, part, part + 2049, ctx->stream));
+    CK(vec_dot(x, gv, m, part, part + 2050, ctx->stream));
+    double h[2] = {0.0, 0.0};
+    CK(cudaMemcpyAsync(h, part + 2049, 2 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    const double alpha = h[1] > 0.0 ? h[0] / h[1] : 0.0;
+    if (!(alpha == alpha) || alpha == 0.0 || std::isinf(alpha)) return HELP_OK;
+    CK(vec_scale(x, alpha, m, ctx->stream));
+    *used = true;
     return HELP_OK;
 }
 
@@ -504,6 +616,15 @@ int renew_impl(help_pcg* ctx, const double* d_host) {
                   mixed ? ctx->dsinv32.as<float>() : nullptr, ctx->stream));
     rc = read_int(ctx, &c->regularised, &ctx->dense_regularised);
     if (rc) return rc;
+    // this renew's solves seed the next renew's warm starts
+    ctx->x2_cur ^= 1;
+    for (int q = 0; q < kSolveSlots; ++q) ctx->x2_have[ctx->x2_cur][q] = false;
+    ctx->solve_slot = 0;
+    ctx->mlp_active = false;
+    if (ctx->mlp) {
+        rc = learned_renew(ctx);
+        if (rc) return rc;
+    }
     CK(cudaGetLastError());
     ctx->renewed = true;
     ctx->have_prev_x2 = false;
@@ -536,7 +657,7 @@ void help_pcg_default_options(help_pcg_options* o) {
     o->inner_max_iter = 200000;
     o->warm_start = 0;
     o->fallback = 1;
-    o->threads = 0;
+    o->cg_path = 0;
 }
 
 int help_pcg_create(const help_pcg_options* opt, help_pcg** out) {
@@ -566,7 +687,6 @@ int help_pcg_create(const help_pcg_options* opt, help_pcg** out) {
         delete ctx;
         return e == cudaErrorMemoryAllocation ? HELP_E_NOMEM : HELP_E_CUDA;
     }
-    ctx->threads = ctx->opt.threads > 0 ? ctx->opt.threads : 512;
     *out = ctx;
     return HELP_OK;
 }
@@ -656,6 +776,10 @@ int help_pcg_construct(help_pcg* ctx, int32_t m, int32_t n, const int32_t* col_p
     CK(ctx->cg_part.ensure(sizeof(double) * 4 * (size_t)ctx->cg_blocks));
     CK(cg_configure<double>(std::max(ctx->opt.pivots, 1)));
     if (mixed) CK(cg_configure<float>(std::max(ctx->opt.pivots, 1)));
+    ctx->cluster_cs[0] = cg_cluster_configure<double>(std::max(ctx->opt.pivots, 1));
+    ctx->cluster_cs[1] = mixed ? cg_cluster_configure<float>(std::max(ctx->opt.pivots, 1)) : 0;
+    ctx->stats.cluster_ctas = ctx->cluster_cs[0];
+    cudaGetLastError();
     ctx->constructed = true;
     ctx->renewed = false;
     return HELP_OK;
@@ -711,7 +835,15 @@ int help_pcg_solve(help_pcg* ctx, const double* d, const double* b_1, const doub
                            ctx->rhs.as<double>(), ctx->b2.as<double>(), nullptr, nullptr, 0.0, spmv_blocks(ctx),
                            kSpmvThreads, ctx->stream));
     // x_2 (UsePCG_CPU.cpp:154-166)
-    const bool warm = ctx->opt.warm_start && ctx->have_prev_x2;
+    const int slot = std::min(ctx->solve_slot, kSolveSlots - 1);
+    bool warm = ctx->opt.warm_start && ctx->have_prev_x2;
+    bool learned_warm = false;
+    if (ctx->mlp_active) {
+        rc = learned_warm_start(ctx, slot, &learned_warm);
+        if (rc) return rc;
+        warm = learned_warm;
+    }
+    const bool learned = ctx->mlp_active;
     long long iters = 0;
     int outer = 0, fell_back = 0, converged = 0;
     rc = normal_solve(ctx, ctx->rhs.as<double>(), ctx->x.as<double>(), warm, &iters, &outer, &fell_back, &converged);
@@ -721,6 +853,34 @@ int help_pcg_solve(help_pcg* ctx, const double* d, const double* b_1, const doub
     rc = residual_f64(ctx, ctx->x.as<double>(), ctx->rhs.as<double>(), ctx->res.as<double>(), &rr);
     if (!rc) rc = sumsq_host(ctx, ctx->rhs.as<double>(), m, &rhs2);
     if (rc) return rc;
+    if (learned) {
+        // the plain preconditioner judges the model: redo cold and uncorrected
+        // on an iteration cap or a failed FP64 residual check
+        const double rel = rhs2 > 0.0 ? std::sqrt(rr / rhs2) : std::sqrt(rr);
+        if (!converged || !(rel <= std::max(1e-6, 100.0 * ctx->opt.cg_tol))) {
+            rc = learned_restore(ctx);
+            if (rc) return rc;
+            long long it2 = 0;
+            int outer2 = 0, fb2 = 0;
+            rc = normal_solve(ctx, ctx->rhs.as<double>(), ctx->x.as<double>(), false, &it2, &outer2, &fb2, &converged);
+            if (rc) return rc;
+            iters += it2;
+            outer += outer2;
+            fell_back = 1;
+            learned_warm = false;
+            ctx->stats.learned_fallbacks++;
+            rc = residual_f64(ctx, ctx->x.as<double>(), ctx->rhs.as<double>(), ctx->res.as<double>(), &rr);
+            if (rc) return rc;
+        }
+    }
+    if (ctx->mlp) {
+        CK(ctx->x2h[ctx->x2_cur][slot].ensure(8 * (size_t)m));
+        CK(cudaMemcpyAsync(ctx->x2h[ctx->x2_cur][slot].p, ctx->x.p, 8 * (size_t)m, cudaMemcpyDeviceToDevice,
+                           ctx->stream));
+        ctx->x2_have[ctx->x2_cur][slot] = true;
+    }
+    ctx->solve_slot++;
+    ctx->stats.learned_warm = learned_warm ? 1 : 0;
     // x_1 = D^-1 (b_1 - A^T x_2) = D^-1/2 (u - B^T x_2)   (UsePCG_CPU.cpp:171-177)
     CK(spmv_launch<double>(kEpiBacksub, view<double>(ctx->pl_csc, ctx->cp, ctx->ri, ctx->bvT), ctx->x.as<double>(),
                            ctx->x1.as<double>(), ctx->u.as<double>(), nullptr, ctx->s.as<double>(), 0.0,
@@ -856,6 +1016,38 @@ int help_pcg_cg(help_pcg* ctx, const double* b, double* x, int64_t* iters) {
     if (rc) return rc;
     if (iters) *iters = res.iterations;
     return d2h(ctx, x, ctx->x.as<double>(), ctx->m);
+}
+
+int help_pcg_attach_mlp(help_pcg* ctx, help_mlp* mlp) {
+    if (!ctx) return HELP_E_ARG;
+    if (mlp && help_mlp_device(mlp) != ctx->device)
+        return fail(ctx, HELP_E_ARG, "attach_mlp: the model lives on another device");
+    if (!mlp && ctx->mlp_active && ctx->renewed) {
+        CK(cudaSetDevice(ctx->device));
+        int rc = learned_restore(ctx);
+        if (rc) return rc;
+        CK(cudaStreamSynchronize(ctx->stream));
+    }
+    ctx->mlp = mlp;
+    return HELP_OK;
+}
+
+int help_pcg_features(help_pcg* ctx, float* x) {
+    if (!ctx || !x) return HELP_E_ARG;
+    if (!ctx->renewed) return fail(ctx, HELP_E_ARG, "features: renew first");
+    CK(cudaSetDevice(ctx->device));
+    // features read D_S of the uncorrected preconditioner
+    double* saved = ctx->res.as<double>();
+    if (ctx->mlp_active) {
+        CK(cudaMemcpyAsync(saved, ctx->dsinv.p, 8 * (size_t)ctx->m, cudaMemcpyDeviceToDevice, ctx->stream));
+        CK(cudaMemcpyAsync(ctx->dsinv.p, ctx->dsinv_plain.p, 8 * (size_t)ctx->m, cudaMemcpyDeviceToDevice, ctx->stream));
+    }
+    int rc = learned_features(ctx, nullptr, x);
+    if (rc) return rc;
+    if (ctx->mlp_active)
+        CK(cudaMemcpyAsync(ctx->dsinv.p, saved, 8 * (size_t)ctx->m, cudaMemcpyDeviceToDevice, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return HELP_OK;
 }
 
 int help_adat_assemble(help_pcg* ctx, const double* w, int32_t* row_ptr, int32_t* col, double* val, int64_t* nnz) {

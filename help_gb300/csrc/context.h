@@ -52,32 +52,12 @@ struct RowPlan {
 constexpr int kGminF64 = 2;  // 2 lanes x 8 B = a 16-byte run per load, sector reuse through L1
 constexpr int kGminF32 = 8;  // 8 lanes x 4 B = one 32-byte sector per load
 
-// Results a CG run leaves behind.
-struct CgOut {
-    long long iterations;
-    double rr0;
-    double rr;
-    int converged;
-    int status;
-};
-
-// Device control block: barrier words, status, CG outputs, top-k state.
-struct Ctrl {
-    unsigned int bar_count;
-    unsigned int bar_gen;
-    int status;
-    int pad;
-    CgOut cg;
-    // radix top-k selection state
-    unsigned long long prefix;     // selected high bits of the threshold key
-    unsigned long long mask;       // bits decided so far
-    int remaining;                 // how many still to take at/below the prefix
-    int n_greater;                 // rows strictly above the final threshold
-    int scratch[2];
-};
-
 constexpr int kTopkBins = 256;
 constexpr int kGraphIters = 8;    // CG iterations per graph launch
+constexpr int kSolveSlots = 4;    // solves per renew whose solutions seed the next renew's
+// auto path: single-cluster CG at or below this work per iteration (measured:
+// faster than the graph on config 0 (77k), slower from ~250k on)
+constexpr int64_t kClusterWorkMax = 150000;
 
 }  // namespace help
 
@@ -128,17 +108,28 @@ struct help_pcg {
 
     const double* last_d = nullptr;
     bool have_prev_x2 = false;
+    bool fp32_stagnated = false;      // mixed: FP32 refinement stalled once; FP64 from then on
+
+    // learned part (mlp_api.cu): attached model, its per-renew inputs and
+    // outputs, the uncorrected D_S^-1, and the solutions of the solve slots
+    // of the current and the previous renew
+    help_mlp* mlp = nullptr;
+    bool mlp_active = false;          // correction applied in this renew (cleared by a fallback)
+    help::DevMem mlp_x, mlp_out, dsinv_plain;
+    help::DevMem x2h[2][help::kSolveSlots];
+    bool x2_have[2][help::kSolveSlots] = {};
+    int x2_cur = 0;
+    int solve_slot = 0;
     help_pcg_stats stats{};
-    int coop_blocks_f64 = 0, coop_blocks_f32 = 0;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     // CG graphs (one per precision), re-captured when their arguments change
     cudaGraphExec_t graph_exec[2] = {nullptr, nullptr};
     std::vector<unsigned char> graph_args[2];
     int cg_blocks = 0;
+    int cluster_cs[2] = {0, 0};       // single-cluster CG: CTAs per cluster (0 = unavailable)
     help::DevMem cg_part;  // 4 x cg_blocks doubles
     help::CgScalars* h_sc = nullptr;  // pinned mirror of the device scalars
     double solve_kernel_ms = 0;       // accumulators for the current solve
     long long solve_iters_f32 = 0;
     int solve_launches = 0;
-    int threads = 512;
 };

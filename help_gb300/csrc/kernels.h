@@ -71,6 +71,11 @@ cudaError_t cg_launch_init(const CgArgs<V>& A, int blocks, cudaStream_t st);
 template <class V>
 cudaError_t cg_launch_iteration(const CgArgs<V>& A, int blocks, cudaStream_t st);
 int cg_threads();
+// Single-cluster CG (small systems): cluster size 16 / 8 / 0 = unavailable.
+template <class V>
+int cg_cluster_configure(int k_max);
+template <class V>
+cudaError_t cg_launch_cluster(const CgArgs<V>& A, int cs, int iters, cudaStream_t st);
 
 // ---- standalone SpMV over items (vec.cu)
 enum SpmvEpi {
@@ -94,6 +99,9 @@ cudaError_t vec_fill(double* x, double v, int64_t n, cudaStream_t st);
 cudaError_t vec_fill_f32(float* x, float v, int64_t n, cudaStream_t st);
 // Deterministic sum of squares into out[0] (uses `part` of >= 1024 doubles).
 cudaError_t vec_sumsq(const double* x, int64_t n, double* part, double* out, cudaStream_t st);
+// Deterministic x . y into out[0] (same scratch as vec_sumsq); x *= a.
+cudaError_t vec_dot(const double* x, const double* y, int64_t n, double* part, double* out, cudaStream_t st);
+cudaError_t vec_scale(double* x, double a, int64_t n, cudaStream_t st);
 
 // ---- renew pipeline (renew.cu)
 // s = d^-1/2 (status <- numeric error if some d_j is not positive and finite)

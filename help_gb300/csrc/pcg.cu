@@ -26,9 +26,13 @@
 //   k_c  : x += alpha p, r -= alpha q, r.r -> stop?, a = W r_P
 // Vectors are V (double, or float for the inner solves of mixed precision);
 // dot products, alpha/beta and the pivot-block work stay in double.
+#include <cooperative_groups.h>
+
 #include "common.cuh"
 #include "kernels.h"
 #include "spmv.cuh"
+
+namespace cg = cooperative_groups;
 
 namespace help {
 
@@ -291,6 +295,189 @@ size_t gemv_smem(const CgArgs<V>& A) {
     return (size_t)(A.k > 0 ? A.k : 1) * sizeof(double);
 }
 
+// ---------------------------------------------------------------- one cluster
+//
+// For small systems the six launches of an iteration cost more than their
+// work.  k_cg_cluster runs whole iterations inside one thread-block cluster
+// (8 or 16 CTAs of 256 threads, one per SM): the same six phases, separated
+// by hardware cluster barriers (barrier.cluster arrive.release /
+// wait.acquire), with the dot products reduced through distributed shared
+// memory -- every CTA reads the CTAs' partials in rank order, so all of them
+// form bit-identical alpha, beta and stopping decisions and leave the loop
+// together.  Vectors written inside the kernel are read with ld.global.cg
+// (L2, coherent across the cluster's SMs); only the matrix and W go through
+// the read-only path.  No CTA ever waits on a flag.
+
+// 256 threads: measured on config 0 (m = 2,000, 30k nonzeros) at 27.7 us per
+// iteration against 30.7 (512) and 39.8 (1024), the block reductions and
+// barriers of the wide CTAs costing more than their extra parallelism.
+constexpr int kClusterThreads = 256;
+
+// Sum over the cluster's CTAs (rank order) of s_part[slot] (+ s_part[slot2]).
+// Call after a cluster barrier that follows every CTA's write of its slots.
+HELP_DEVINL double cluster_total(cg::cluster_group& cl, double* s_part, int slot, int slot2, double* s_out) {
+    if (threadIdx.x < 32) {
+        const unsigned int lane = threadIdx.x;
+        double v = 0.0;
+        if (lane < cl.num_blocks()) {
+            const double* rp = cl.map_shared_rank(s_part, lane);
+            v = rp[slot];
+            if (slot2 >= 0) v += rp[slot2];
+        }
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const double t = __shfl_down_sync(0xffffffffu, v, o);
+            if ((lane & (2 * o - 1)) == 0) v += t;
+        }
+        if (lane == 0) *s_out = v;
+    }
+    __syncthreads();
+    return *s_out;
+}
+
+template <class V>
+__global__ void __launch_bounds__(kClusterThreads) k_cg_cluster(const CgArgs<V> A, int iters) {
+    cg::cluster_group cl = cg::this_cluster();
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    double* s_vec = reinterpret_cast<double*>(smem_raw);
+    __shared__ double red[kClusterThreads];
+    __shared__ double s_part[4];
+    __shared__ double s_tot[4];
+    CgScalars* sc = A.sc;
+    if (*(volatile const int*)&sc->done != 0) return;  // same value in every CTA (written before this launch)
+    const int tid = threadIdx.x;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    long long it = sc->it;
+    double rz_old = sc->rz_old, rz = sc->rz, rr = sc->rr, alpha = sc->alpha, beta = sc->beta;
+    const double term2 = sc->term2;
+    const long long max_it = sc->max_iter;
+    const bool has_delta = (A.delta != 0.0);
+    const V vd = (V)A.delta;
+    int done = 0;
+    for (int u = 0; u < iters && done == 0; ++u) {
+        const V* r = (it & 1) ? A.r1 : A.r0;
+        V* rn = (it & 1) ? A.r0 : A.r1;
+        const V* p = (it & 1) ? A.p1 : A.p0;
+        V* pn = (it & 1) ? A.p0 : A.p1;
+        // P2: z_N = D_S^-1 (r_N - C a)
+        double prz = 0.0;
+        spmv_rows<V>(
+            A.c, [&](int c) { return (V)__ldcg(A.a + c); },
+            [&](int i, V s) {
+                if (A.pivpos[i] < 0) {
+                    const V ri = __ldcg(r + i);
+                    const V zi = A.dsinv[i] * (ri - s);
+                    A.z[i] = zi;
+                    prz = fma((double)ri, (double)zi, prz);
+                }
+            },
+            red);
+        prz = block_sum(prz, red);
+        if (tid == 0) s_part[0] = prz;
+        cl.sync();
+        // P3: w = r_P - C^T z_N
+        double paw = 0.0;
+        spmv_rows<V>(
+            A.ct, [&](int i) { return __ldcg(A.z + i); },
+            [&](int c, V s) {
+                const double wc = (double)__ldcg(r + A.piv[c]) - (double)s;
+                A.w[c] = wc;
+                paw = fma(__ldcg(A.a + c), wc, paw);
+            },
+            red);
+        paw = block_sum(paw, red);
+        if (tid == 0) s_part[1] = paw;
+        cl.sync();
+        rz = cluster_total(cl, s_part, 0, 1, &s_tot[0]);
+        if (!(rz > 0.0)) {
+            done = 3;
+            break;
+        }
+        beta = (it == 0) ? 0.0 : rz / rz_old;
+        // P4: z_P = W w, p_new = z + beta p
+        {
+            const bool first = (it == 0);
+            const V vb = (V)beta;
+            gemv_rows(A.k, A.W, [&](int c) { return __ldcg(A.w + c); },
+                      [&](int c, double s) {
+                          const int i = A.piv[c];
+                          const V zc = (V)s;
+                          pn[i] = first ? zc : fma_t(vb, __ldcg(p + i), zc);
+                      },
+                      s_vec);
+            for (long long i = blockIdx.x * (long long)blockDim.x + tid; i < A.m; i += stride) {
+                if (A.pivpos[i] < 0) {
+                    const V zi = __ldcg(A.z + i);
+                    pn[i] = first ? zi : fma_t(vb, __ldcg(p + i), zi);
+                }
+            }
+        }
+        cl.sync();
+        // A: t = B^T p_new
+        spmv_rows<V>(A.csc, [&](int i) { return __ldcg(pn + i); }, [&](int j, V s) { A.t[j] = s; }, red);
+        cl.sync();
+        // B: q = B t + delta p_new
+        double ppq = 0.0;
+        spmv_rows<V>(
+            A.csr, [&](int j) { return __ldcg(A.t + j); },
+            [&](int i, V s) {
+                const V pi = __ldcg(pn + i);
+                const V qi = has_delta ? fma_t(vd, pi, s) : s;
+                A.q[i] = qi;
+                ppq = fma((double)pi, (double)qi, ppq);
+            },
+            red);
+        ppq = block_sum(ppq, red);
+        if (tid == 0) s_part[2] = ppq;
+        cl.sync();
+        const double pq = cluster_total(cl, s_part, 2, -1, &s_tot[1]);
+        if (!(pq > 0.0)) {
+            done = 3;
+            break;
+        }
+        alpha = rz / pq;
+        rz_old = rz;
+        // C: x += alpha p_new, r_new = r - alpha q, a = W r_new_P
+        {
+            const V va = (V)alpha;
+            double prr = 0.0;
+            for (long long i = blockIdx.x * (long long)blockDim.x + tid; i < A.m; i += stride) {
+                const V pi = __ldcg(pn + i), qi = __ldcg(A.q + i);
+                A.x[i] = fma_t(va, pi, __ldcg(A.x + i));
+                const V ri = fma_t(-va, qi, __ldcg(r + i));
+                rn[i] = ri;
+                prr = fma((double)ri, (double)ri, prr);
+            }
+            prr = block_sum(prr, red);
+            gemv_rows(A.k, A.W,
+                      [&](int c) {
+                          const int i = A.piv[c];
+                          return (double)fma_t(-va, __ldcg(A.q + i), __ldcg(r + i));
+                      },
+                      [&](int c, double s) { A.a[c] = s; }, s_vec);
+            if (tid == 0) s_part[3] = prr;
+        }
+        cl.sync();
+        rr = cluster_total(cl, s_part, 3, -1, &s_tot[2]);
+        ++it;
+        if (!(rr == rr)) done = 3;
+        else if (rr < term2 || rr == 0.0) done = 1;
+        else if (it >= max_it) done = 2;
+    }
+    // no CTA may exit while another can still read its shared memory
+    cl.sync();
+    if (cl.block_rank() == 0 && tid == 0) {
+        sc->it = it;
+        sc->rr = rr;
+        sc->rz = rz;
+        sc->rz_old = rz_old;
+        sc->alpha = alpha;
+        sc->beta = beta;
+        if (done == 3) sc->status = kStatusNumeric;
+        if (done != 0) sc->done = done;
+    }
+}
+
 }  // namespace
 
 template <class V>
@@ -323,11 +510,65 @@ cudaError_t cg_launch_iteration(const CgArgs<V>& A, int blocks, cudaStream_t st)
 
 int cg_threads() { return kCgThreads; }
 
+// Cluster size for k_cg_cluster: 16 CTAs where the GPU can co-schedule such a
+// cluster with this shared memory, else 8 (the portable size); 0 if neither.
+template <class V>
+int cg_cluster_configure(int k_max) {
+    const int smem = (k_max > 0 ? k_max : 1) * (int)sizeof(double);
+    if (cudaFuncSetAttribute(k_cg_cluster<V>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess)
+        return 0;
+    for (int cs : {16, 8}) {
+        if (cs > 8 && cudaFuncSetAttribute(k_cg_cluster<V>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) !=
+                          cudaSuccess) {
+            cudaGetLastError();
+            continue;
+        }
+        cudaLaunchConfig_t cfg = {};
+        cudaLaunchAttribute at[1];
+        at[0].id = cudaLaunchAttributeClusterDimension;
+        at[0].val.clusterDim.x = cs;
+        at[0].val.clusterDim.y = 1;
+        at[0].val.clusterDim.z = 1;
+        cfg.gridDim = dim3(cs);
+        cfg.blockDim = dim3(kClusterThreads);
+        cfg.dynamicSmemBytes = smem;
+        cfg.attrs = at;
+        cfg.numAttrs = 1;
+        int nclusters = 0;
+        if (cudaOccupancyMaxActiveClusters(&nclusters, k_cg_cluster<V>, &cfg) == cudaSuccess && nclusters >= 1)
+            return cs;
+        cudaGetLastError();
+    }
+    return 0;
+}
+
+// Up to `iters` CG iterations in one launch of one cluster of `cs` CTAs.
+template <class V>
+cudaError_t cg_launch_cluster(const CgArgs<V>& A, int cs, int iters, cudaStream_t st) {
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = cs;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.gridDim = dim3(cs);
+    cfg.blockDim = dim3(kClusterThreads);
+    cfg.dynamicSmemBytes = gemv_smem(A);
+    cfg.stream = st;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, k_cg_cluster<V>, A, iters);
+}
+
 template cudaError_t cg_configure<double>(int);
 template cudaError_t cg_configure<float>(int);
 template cudaError_t cg_launch_init<double>(const CgArgs<double>&, int, cudaStream_t);
 template cudaError_t cg_launch_init<float>(const CgArgs<float>&, int, cudaStream_t);
 template cudaError_t cg_launch_iteration<double>(const CgArgs<double>&, int, cudaStream_t);
 template cudaError_t cg_launch_iteration<float>(const CgArgs<float>&, int, cudaStream_t);
+template int cg_cluster_configure<double>(int);
+template int cg_cluster_configure<float>(int);
+template cudaError_t cg_launch_cluster<double>(const CgArgs<double>&, int, int, cudaStream_t);
+template cudaError_t cg_launch_cluster<float>(const CgArgs<float>&, int, int, cudaStream_t);
 
 }  // namespace help

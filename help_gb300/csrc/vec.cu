@@ -69,6 +69,19 @@ __global__ void k_sumsq_part(const double* __restrict__ x, int64_t n, double* __
     s = block_sum(s, red);
     if (threadIdx.x == 0) part[blockIdx.x] = s;
 }
+__global__ void k_dot_part(const double* __restrict__ x, const double* __restrict__ y, int64_t n,
+                           double* __restrict__ part) {
+    __shared__ double red[1024];
+    double s = 0.0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        s = fma(x[i], y[i], s);
+    s = block_sum(s, red);
+    if (threadIdx.x == 0) part[blockIdx.x] = s;
+}
+__global__ void k_scale(double* __restrict__ x, double a, int64_t n) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        x[i] *= a;
+}
 __global__ void k_sum_parts(const double* __restrict__ part, int np, double* __restrict__ out) {
     __shared__ double red[1024];
     double s = 0.0;
@@ -141,6 +154,16 @@ cudaError_t vec_fill(double* x, double v, int64_t n, cudaStream_t st) {
 }
 cudaError_t vec_fill_f32(float* x, float v, int64_t n, cudaStream_t st) {
     k_fill_f32<<<grid_for(n, 256), 256, 0, st>>>(x, v, n);
+    return cudaGetLastError();
+}
+cudaError_t vec_dot(const double* x, const double* y, int64_t n, double* part, double* out, cudaStream_t st) {
+    const int nb = 1024;
+    k_dot_part<<<nb, 256, 0, st>>>(x, y, n, part);
+    k_sum_parts<<<1, 1024, 0, st>>>(part, nb, out);
+    return cudaGetLastError();
+}
+cudaError_t vec_scale(double* x, double a, int64_t n, cudaStream_t st) {
+    k_scale<<<grid_for(n, 256), 256, 0, st>>>(x, a, n);
     return cudaGetLastError();
 }
 cudaError_t vec_sumsq(const double* x, int64_t n, double* part, double* out, cudaStream_t st) {

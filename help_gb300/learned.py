@@ -1,0 +1,324 @@
+"""The learned part: per-row MLP giving a Schur-diagonal correction and a
+warm-start scale for the normal-equations PCG (include/help_gpu.h, HELP_MLP_*).
+
+Pipeline, all on the GPU through the library's own kernels:
+  1. ``collect``: run the HSD interior-point method with the plain FP64 PCG
+     backend on seeded LPs; after every renew record the raw per-row features
+     (device kernel, help_pcg_features), the pivots and the solutions x_2 of
+     every solve slot;
+  2. ``targets``: per row, (0) the log-ratio of a 2-norm equilibrated diagonal
+     of the Schur complement S (non-pivot block) to diag(S) -- computed from
+     the dense S, so for small systems only -- and (1) the ratio of this
+     renew's x_2 to the previous renew's x_2 of the same slot, weighted by the
+     square of the latter (the loss is then || o1 .* x_prev - x_now ||^2);
+  3. ``train``: full-batch Adam on the weighted squared error with the
+     library's BF16 forward / backward kernels (help_mlp_train_step);
+  4. ``evaluate``: the same IPM with and without the model attached.
+
+Instances are scaled-down multicommodity-flow LPs of the benchmark's family
+(grid graphs, several commodities); the dense targets bound their size.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import time
+
+import numpy as np
+
+from . import native
+from .backend import GpuNormalEquations
+
+
+def _torch():
+    import torch
+
+    return torch
+
+
+def bf16_bits(x: np.ndarray) -> np.ndarray:
+    """float32 -> BF16 bit patterns (uint16), round to nearest even."""
+    u = np.ascontiguousarray(x, dtype=np.float32).view(np.uint32).astype(np.uint64)
+    u = (u + 0x7FFF + ((u >> 16) & 1)) >> 16
+    return u.astype(np.uint16)
+
+
+class Mlp:
+    """A model on one GPU (help_mlp)."""
+
+    def __init__(self, device: int = 0, params: np.ndarray | None = None):
+        self.lib = native.gpu_lib()
+        h = C.c_void_p()
+        rc = self.lib.help_mlp_create(device, C.byref(h))
+        if rc != native.HELP_OK:
+            raise RuntimeError("help_mlp_create failed (%d)" % rc)
+        self.h = h
+        self.device = device
+        if params is not None:
+            self.set_params(params)
+
+    def _check(self, rc: int) -> None:
+        if rc != native.HELP_OK:
+            raise RuntimeError("help_mlp: %s (%d)" % (self.lib.help_mlp_last_error(self.h).decode(), rc))
+
+    def close(self) -> None:
+        if self.h:
+            self.lib.help_mlp_free(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_params(self, p: np.ndarray) -> None:
+        p = np.ascontiguousarray(p, dtype=np.float32)
+        assert p.shape == (native.MLP_PARAMS,)
+        self._check(self.lib.help_mlp_set_params(self.h, p.ctypes.data))
+
+    def get_params(self) -> np.ndarray:
+        p = np.empty(native.MLP_PARAMS, np.float32)
+        self._check(self.lib.help_mlp_get_params(self.h, p.ctypes.data))
+        return p
+
+    # device tensors (torch) in, as the C ABI takes device pointers
+    def forward(self, x_bits, rows: int):
+        torch = _torch()
+        out = torch.empty((rows, native.MLP_OUT), dtype=torch.float32, device=x_bits.device)
+        self._check(self.lib.help_mlp_forward(self.h, x_bits.data_ptr(), rows, out.data_ptr(),
+                                              torch.cuda.current_stream().cuda_stream))
+        torch.cuda.synchronize()
+        return out
+
+    def loss_grad(self, x_bits, t, w, rows: int):
+        loss = C.c_double()
+        g = np.empty(native.MLP_OFF_MEAN, np.float32)
+        self._check(self.lib.help_mlp_loss_grad(self.h, x_bits.data_ptr(), t.data_ptr(), w.data_ptr(), rows,
+                                                C.byref(loss), g.ctypes.data))
+        return loss.value, g
+
+    def train_step(self, x_bits, t, w, rows: int, lr: float) -> float:
+        loss = C.c_double()
+        self._check(self.lib.help_mlp_train_step(self.h, x_bits.data_ptr(), t.data_ptr(), w.data_ptr(), rows,
+                                                 C.c_float(lr), C.byref(loss)))
+        return loss.value
+
+
+def init_params(seed: int, mean=None, scale=None) -> np.ndarray:
+    """He-style initial weights, zero biases except the warm-start scale's (1)."""
+    rng = np.random.default_rng(seed)
+    In, H, O = native.MLP_IN, native.MLP_HIDDEN, native.MLP_OUT
+    p = np.zeros(native.MLP_PARAMS, np.float32)
+    p[native.MLP_OFF_W1:native.MLP_OFF_B1] = rng.normal(0, np.sqrt(2.0 / In), H * In)
+    p[native.MLP_OFF_W2:native.MLP_OFF_B2] = rng.normal(0, np.sqrt(2.0 / H), H * H)
+    p[native.MLP_OFF_W3:native.MLP_OFF_B3] = rng.normal(0, 0.1 * np.sqrt(1.0 / H), O * H)
+    p[native.MLP_OFF_B3 + 1] = 1.0
+    p[native.MLP_OFF_MEAN:native.MLP_OFF_SCALE] = 0.0 if mean is None else mean
+    p[native.MLP_OFF_SCALE:] = 1.0 if scale is None else scale
+    return p
+
+
+def zero_params() -> np.ndarray:
+    """A model whose outputs are 0: no correction, no warm start (alpha = 0)."""
+    p = np.zeros(native.MLP_PARAMS, np.float32)
+    p[native.MLP_OFF_SCALE:] = 1.0
+    return p
+
+
+class _Recorder:
+    """NeBackend whose entry points call a GPU backend and record each renew."""
+
+    def __init__(self, ne: GpuNormalEquations, m: int, n: int):
+        self.ne, self.m, self.n = ne, m, n
+        self.renews: list[dict] = []
+        torch = _torch()
+        self._feat = torch.empty((m, native.MLP_IN), dtype=torch.float32, device="cuda:%d" % ne.options.device)
+        lib, ctx = ne.lib, ne.ctx
+        self.error: BaseException | None = None
+
+        def guarded(fn):
+            # an exception must not cross the C driver: keep it, report failure
+            def call(*a):
+                try:
+                    return fn(*a)
+                except BaseException as e:  # noqa: BLE001
+                    self.error = e
+                    return native.HELP_E_ARG
+            return call
+
+        @guarded
+        def construct(_c, m_, n_, cp, ri, v):
+            ne.m, ne.n = int(m_), int(n_)
+            return lib.help_pcg_construct(ctx, m_, n_, cp, ri, v)
+
+        @guarded
+        def renew(_c, d):
+            rc = lib.help_pcg_renew(ctx, d)
+            if rc == native.HELP_OK:
+                self._snapshot(d)
+            return rc
+
+        @guarded
+        def solve(_c, d, b1, b2, x1, x2):
+            rc = lib.help_pcg_solve(ctx, d, b1, b2, x1, x2)
+            if rc == native.HELP_OK and self.renews:
+                x = np.ctypeslib.as_array(C.cast(x2, C.POINTER(C.c_double)), (self.m,)).copy()
+                self.renews[-1]["x2"].append(x)
+            return rc
+
+        @guarded
+        def destruct(_c):
+            return lib.help_pcg_destruct(ctx)
+
+        self._fns = (native.CONSTRUCT_FN(construct), native.RENEW_FN(renew), native.SOLVE_FN(solve),
+                     native.DESTRUCT_FN(destruct))
+
+    def _snapshot(self, d_ptr) -> None:
+        ne = self.ne
+        rc = ne.lib.help_pcg_features(ne.ctx, self._feat.data_ptr())
+        if rc != native.HELP_OK:
+            raise RuntimeError("help_pcg_features failed (%d)" % rc)
+        piv, dg, ds = ne.pivots()
+        d = np.ctypeslib.as_array(C.cast(d_ptr, C.POINTER(C.c_double)), (self.n,)).copy()
+        self.renews.append({"feat": self._feat.cpu().numpy().copy(), "piv": piv.copy(), "diag": dg.copy(),
+                            "ds": ds.copy(), "d": d, "x2": []})
+
+    def backend(self) -> native.NeBackend:
+        f = lambda fn: C.cast(fn, C.c_void_p).value
+        return native.NeBackend(ctx=None, construct=f(self._fns[0]), renew=f(self._fns[1]), solve=f(self._fns[2]),
+                                destruct=f(self._fns[3]))
+
+
+def collect(lp, pivots: int, cg_tol: float = 1e-10, device: int = 0) -> list[dict]:
+    """Renews of one IPM run of ``lp`` with the plain PCG (a zero model attached
+    so the solutions of every slot are kept for the next renew's features)."""
+    from . import hsd
+
+    zero = Mlp(device, zero_params())
+    with GpuNormalEquations(pivots=pivots, cg_tol=cg_tol, cg_max_iter=200_000, device=device) as ne:
+        ne._check(ne.lib.help_pcg_attach_mlp(ne.ctx, zero.h))
+        rec = _Recorder(ne, lp.m, lp.n)
+        res = hsd.solve_lp(lp, rec.backend())
+        ne._check(ne.lib.help_pcg_attach_mlp(ne.ctx, None))
+    zero.close()
+    if rec.error is not None:
+        raise RuntimeError("recording the IPM run failed: %r" % (rec.error,)) from rec.error
+    if res["rc"] != 0 or res["status"] != 0:
+        raise RuntimeError("IPM failed while collecting (rc %d, status %d)" % (res["rc"], res["status"]))
+    return rec.renews
+
+
+def _dense(lp) -> np.ndarray:
+    A = np.zeros((lp.m, lp.n))
+    for j in range(lp.n):
+        A[lp.row_ind[lp.col_ptr[j]:lp.col_ptr[j + 1]], j] = lp.val[lp.col_ptr[j]:lp.col_ptr[j + 1]]
+    return A
+
+
+def equilibrated_log_ratio(S: np.ndarray, iters: int = 8) -> np.ndarray:
+    """ln(e_i / S_ii) for the diagonal e that 2-norm-equilibrates S symmetrically."""
+    e = np.diag(S).copy()
+    for _ in range(iters):
+        sc = 1.0 / np.sqrt(e)
+        rn = np.sqrt(((S * sc[None, :] * sc[:, None]) ** 2).sum(1))
+        e = e * rn
+    return np.log(e / np.diag(S))
+
+
+def targets(lp, renews: list[dict], dense_max: int = 4000) -> dict:
+    """Training rows (raw features, targets, weights) of one IPM run."""
+    if lp.m > dense_max:
+        raise ValueError("dense Schur targets need m <= %d" % dense_max)
+    A = _dense(lp)
+    X, T, W = [], [], []
+    for r in range(1, len(renews)):
+        cur, prev = renews[r], renews[r - 1]
+        G = (A / cur["d"]) @ A.T
+        piv = cur["piv"]
+        mask = np.ones(lp.m, bool)
+        mask[piv] = False
+        N = np.where(mask)[0]
+        t0 = np.zeros(lp.m)
+        if len(piv):
+            Wi = np.linalg.inv(G[np.ix_(piv, piv)])
+            Cn = G[np.ix_(N, piv)]
+            S = G[np.ix_(N, N)] - Cn @ Wi @ Cn.T
+        else:
+            S = G[np.ix_(N, N)]
+        t0[N] = equilibrated_log_ratio(S)
+        for s in range(min(len(cur["x2"]), len(prev["x2"]))):
+            xp, xc = prev["x2"][s], cur["x2"][s]
+            w1 = xp * xp
+            tot = w1.sum()
+            if not tot > 0:
+                continue
+            ratio = np.where(w1 > 0, xc / np.where(xp != 0, xp, 1.0), 0.0)
+            t = np.stack([t0, np.clip(ratio, -10.0, 10.0)], 1)
+            w = np.stack([mask / max(len(N), 1) if s == 0 else np.zeros(lp.m), w1 / tot], 1)
+            X.append(cur["feat"])
+            T.append(t)
+            W.append(w)
+    return {"X": np.concatenate(X).astype(np.float32), "T": np.concatenate(T).astype(np.float32),
+            "W": np.concatenate(W).astype(np.float32)}
+
+
+def normalisation(X: np.ndarray) -> tuple[np.ndarray, np.ndarray]:
+    mean = np.zeros(native.MLP_IN, np.float32)
+    scale = np.ones(native.MLP_IN, np.float32)
+    mean[:9] = X[:, :9].mean(0)
+    sd = X[:, :9].std(0)
+    scale[:9] = np.where(sd > 1e-6, 1.0 / np.maximum(sd, 1e-6), 1.0)
+    return mean, scale
+
+
+def normalise_bits(X: np.ndarray, mean: np.ndarray, scale: np.ndarray) -> np.ndarray:
+    """The device feature kernel's normalisation and BF16 rounding, on the host."""
+    Z = ((X.astype(np.float32) - mean) * scale).astype(np.float32)
+    Z[:, 9:] = 0.0
+    return bf16_bits(Z)
+
+
+def train(data: dict, steps: int = 600, lr: float = 3e-3, seed: int = 0, device: int = 0,
+          log=None) -> tuple[np.ndarray, list[float]]:
+    """Full-batch Adam with the library's kernels; returns (params, losses)."""
+    torch = _torch()
+    mean, scale = normalisation(data["X"])
+    p0 = init_params(seed, mean, scale)
+    mlp = Mlp(device, p0)
+    dev = torch.device("cuda", device)
+    xb = torch.from_numpy(normalise_bits(data["X"], mean, scale).view(np.int16)).to(dev)
+    t = torch.from_numpy(data["T"]).to(dev)
+    w = torch.from_numpy(data["W"]).to(dev)
+    rows = data["X"].shape[0]
+    losses = []
+    for it in range(steps):
+        step_lr = lr * (0.1 ** (it / max(steps, 1)))
+        losses.append(mlp.train_step(xb, t, w, rows, step_lr))
+        if log and (it % 100 == 0 or it == steps - 1):
+            log("step %d loss %.6g" % (it, losses[-1]))
+    params = mlp.get_params()
+    mlp.close()
+    return params, losses
+
+
+def evaluate(lp, pivots: int, params: np.ndarray | None, cg_tol: float = 1e-10, device: int = 0) -> dict:
+    """One IPM run; with ``params`` the model is attached."""
+    from . import hsd
+
+    mlp = Mlp(device, params) if params is not None else None
+    with GpuNormalEquations(pivots=pivots, cg_tol=cg_tol, cg_max_iter=200_000, device=device) as ne:
+        if mlp is not None:
+            ne._check(ne.lib.help_pcg_attach_mlp(ne.ctx, mlp.h))
+        t0 = time.perf_counter()
+        r = hsd.solve_lp(lp, ne.ne_backend())
+        wall = time.perf_counter() - t0
+        st = ne.stats()
+        if mlp is not None:
+            ne._check(ne.lib.help_pcg_attach_mlp(ne.ctx, None))
+    if mlp is not None:
+        mlp.close()
+    if r["rc"] != 0:
+        raise RuntimeError("IPM backend error (rc %d)" % r["rc"])
+    return {"status": r["status"], "iterations": r["iterations"], "primal_obj": r["primal_obj"],
+            "rel_gap": r["rel_gap"], "cg_iterations": int(st["cg_iterations_total"]), "seconds": wall,
+            "learned_fallbacks": int(st["learned_fallbacks"])}

@@ -12,6 +12,11 @@ import os
 _PKG = os.path.dirname(os.path.abspath(__file__))
 LIBDIR = os.path.join(_PKG, "_lib")
 
+# ---- learned part (help_gpu.h HELP_MLP_*)
+MLP_IN, MLP_HIDDEN, MLP_OUT = 16, 64, 2
+MLP_OFF_W1, MLP_OFF_B1, MLP_OFF_W2, MLP_OFF_B2, MLP_OFF_W3, MLP_OFF_B3 = 0, 1024, 1088, 5184, 5248, 5376
+MLP_OFF_MEAN, MLP_OFF_SCALE, MLP_PARAMS = 5378, 5394, 5410
+
 # ---- error codes (help_gpu.h)
 HELP_OK = 0
 HELP_E_ARG = -1
@@ -53,7 +58,7 @@ class PcgOptions(C.Structure):
         ("inner_max_iter", C.c_int64),
         ("warm_start", C.c_int32),
         ("fallback", C.c_int32),
-        ("threads", C.c_int32),
+        ("cg_path", C.c_int32),
     ]
 
 
@@ -76,6 +81,10 @@ class PcgStats(C.Structure):
         ("cg_iterations_fp32", C.c_int64),
         ("cg_launches", C.c_int32),
         ("dense_regularised", C.c_int32),
+        ("cg_path_used", C.c_int32),
+        ("cluster_ctas", C.c_int32),
+        ("learned_warm", C.c_int32),
+        ("learned_fallbacks", C.c_int32),
     ]
 
 
@@ -168,6 +177,8 @@ GPU_SYMBOLS = [
     "help_pcg_renew", "help_pcg_solve", "help_pcg_destruct", "help_pcg_get_stats",
     "help_pcg_last_error", "help_pcg_matvec", "help_pcg_matvec_dev", "help_pcg_precond_apply",
     "help_pcg_get_pivots", "help_pcg_cg", "help_adat_assemble", "help_adat_matvec_noalloc",
+    "help_mlp_create", "help_mlp_free", "help_mlp_last_error", "help_mlp_set_params", "help_mlp_get_params",
+    "help_mlp_forward", "help_mlp_loss_grad", "help_mlp_train_step", "help_pcg_attach_mlp", "help_pcg_features",
 ]
 LP_SYMBOLS = [
     "help_lp_generate", "help_lp_free", "help_lp_write_mps", "help_csc_to_csr",
@@ -211,6 +222,17 @@ def gpu_lib() -> C.CDLL:
         lib.help_pcg_cg.argtypes = [vp, dp, dp, C.POINTER(C.c_int64)]
         lib.help_adat_assemble.argtypes = [vp, dp, dp, dp, dp, C.POINTER(C.c_int64)]
         lib.help_adat_matvec_noalloc.argtypes = [i32, i32, i64] + [vp] * 10
+        lib.help_mlp_create.argtypes = [i32, C.POINTER(C.c_void_p)]
+        lib.help_mlp_free.argtypes = [vp]
+        lib.help_mlp_last_error.argtypes = [vp]
+        lib.help_mlp_last_error.restype = C.c_char_p
+        lib.help_mlp_set_params.argtypes = [vp, dp]
+        lib.help_mlp_get_params.argtypes = [vp, dp]
+        lib.help_mlp_forward.argtypes = [vp, vp, i64, vp, vp]
+        lib.help_mlp_loss_grad.argtypes = [vp, vp, vp, vp, i64, C.POINTER(C.c_double), dp]
+        lib.help_mlp_train_step.argtypes = [vp, vp, vp, vp, i64, C.c_float, C.POINTER(C.c_double)]
+        lib.help_pcg_attach_mlp.argtypes = [vp, vp]
+        lib.help_pcg_features.argtypes = [vp, vp]
         for s in GPU_SYMBOLS:
             getattr(lib, s)
         _gpu = lib

@@ -60,7 +60,9 @@ typedef struct help_pcg_options {
     /* warm start / learned correction */
     int32_t warm_start;      /* 1: start CG from the previous solve's x_2 of this renew */
     int32_t fallback;        /* 1: on cap or failed FP64 check, redo with plain FP64 PCG */
-    int32_t threads;         /* reserved (ignored; kernels size their own blocks)       */
+    int32_t cg_path;         /* 0 auto: one thread-block cluster runs whole CG iterations
+                                when the system is small, else the multi-kernel graph;
+                                1 always the graph; 2 always the cluster kernel          */
 } help_pcg_options;
 
 typedef struct help_pcg_stats {
@@ -80,6 +82,10 @@ typedef struct help_pcg_stats {
     int64_t cg_iterations_fp32;  /* last solve: iterations run in FP32 (mixed)          */
     int32_t cg_launches;         /* last solve                                          */
     int32_t dense_regularised;   /* last renew: pivots raised to the floor in G11       */
+    int32_t cg_path_used;        /* last CG run: 1 multi-kernel graph, 2 single cluster */
+    int32_t cluster_ctas;        /* CTAs per cluster of the single-cluster path (0 = unavailable) */
+    int32_t learned_warm;        /* last solve: started from the model's warm start     */
+    int32_t learned_fallbacks;   /* since construct: model-assisted solves redone plain */
 } help_pcg_stats;
 
 /* Fills *opt with the defaults (FP64, k = 10, cg_tol = 1e-20 as the reference). */
@@ -146,6 +152,64 @@ int help_pcg_cg(help_pcg* ctx, const double* b, double* x, int64_t* iters);
  * col == NULL only *nnz is returned; then pass arrays of that size. */
 int help_adat_assemble(help_pcg* ctx, const double* w, int32_t* row_ptr, int32_t* col, double* val,
                        int64_t* nnz);
+
+/* ---- learned part (no counterpart in the reference) ----
+ *
+ * A 16 -> 64 -> 64 -> 2 MLP (ReLU, BF16 weights and activations, FP32
+ * accumulation on the tensor cores) reads per-row features of the normal
+ * equations after each renew and gives, per row, (0) the log-factor of a
+ * correction of the preconditioner's Schur diagonal D_S (clamped to +-2) and
+ * (1) a scale of the warm start: solve s of a renew starts from
+ * alpha * (out[:,1] .* x_2 of solve s of the previous renew), alpha the
+ * G-norm-optimal scalar.  The plain partial-Cholesky PCG is its fallback: a
+ * solve that hits the iteration cap or whose FP64 residual check fails is
+ * redone cold with the uncorrected preconditioner.
+ *
+ * Features (row i of A, d = D):  0 log10 diag(A D^-1 A^T)_ii,  1-4 mean /
+ * std / min / max of log10 d_j over the row,  5 log2(1 + row length),
+ * 6 log10(D_S,i / diag_i) (0 on pivot rows),  7 pivot flag,  8 x_2 of the
+ * previous renew's first solve over its RMS;  9-15 zero.  Each is normalised
+ * as (f - mean) * scale with the model's constants, then rounded to BF16.
+ *
+ * Parameters (FP32, HELP_MLP_PARAMS floats): W1[64][16], b1[64], W2[64][64],
+ * b2[64], W3[2][64], b3[2] (row-major, out x in), then the normalisation
+ * mean[16], scale[16].  Training minimises sum w (out - target)^2 / sum w
+ * over rows x 2 entries with Adam (0.9, 0.999, 1e-8) on the trainable part. */
+#define HELP_MLP_IN 16
+#define HELP_MLP_HIDDEN 64
+#define HELP_MLP_OUT 2
+#define HELP_MLP_OFF_W1 0
+#define HELP_MLP_OFF_B1 1024
+#define HELP_MLP_OFF_W2 1088
+#define HELP_MLP_OFF_B2 5184
+#define HELP_MLP_OFF_W3 5248
+#define HELP_MLP_OFF_B3 5376
+#define HELP_MLP_OFF_MEAN 5378
+#define HELP_MLP_OFF_SCALE 5394
+#define HELP_MLP_PARAMS 5410
+
+typedef struct help_mlp help_mlp;
+int help_mlp_create(int32_t device, help_mlp** out);
+int help_mlp_free(help_mlp* mlp);
+const char* help_mlp_last_error(const help_mlp* mlp);
+/* host arrays of HELP_MLP_PARAMS floats; set also resets the Adam state */
+int help_mlp_set_params(help_mlp* mlp, const float* params);
+int help_mlp_get_params(help_mlp* mlp, float* params);
+/* device arrays: x BF16 [rows][16], out FP32 [rows][2]; runs on `stream` */
+int help_mlp_forward(help_mlp* mlp, const void* x, int64_t rows, float* out, void* stream);
+/* device x, target, weight ([rows][2]); host loss and grad (HELP_MLP_OFF_MEAN floats) */
+int help_mlp_loss_grad(help_mlp* mlp, const void* x, const float* target, const float* weight, int64_t rows,
+                       double* loss, float* grad);
+/* one Adam step with learning rate lr on that loss (loss before the step) */
+int help_mlp_train_step(help_mlp* mlp, const void* x, const float* target, const float* weight, int64_t rows,
+                        float lr, double* loss);
+/* Use `mlp` in this context's solves from the next renew on (NULL: plain PCG).
+ * The model must live on the context's device and outlive the attachment. */
+int help_pcg_attach_mlp(help_pcg* ctx, help_mlp* mlp);
+/* Raw (unnormalised) FP32 features of the current renew into the device
+ * array x [m][16]; the previous renew's first solution is used when a model
+ * was attached during it. */
+int help_pcg_features(help_pcg* ctx, float* x);
 
 /* ---- no-allocation product (no counterpart in the reference) ----
  *

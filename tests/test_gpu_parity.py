@@ -83,26 +83,31 @@ def test_pivots_diag_schur_precond(case, k):
         assert rel(z, pc.apply(r)) < 1e-8
 
 
-def test_cg_matches_oracle(case):
+@pytest.mark.parametrize("path", ["graph", "cluster"])
+def test_cg_matches_oracle(case, path):
     name, lp, d, rng = case
     rp, ci, v = lp.csr()
     k = 16
     b = rng.standard_normal(lp.m)
-    with backend.GpuNormalEquations(pivots=k, cg_tol=1e-10, cg_max_iter=20000) as g:
+    with backend.GpuNormalEquations(pivots=k, cg_tol=1e-10, cg_max_iter=20000, cg_path=path) as g:
         g.LinearEquation_Construct(lp)
         g.RenewLinearEquation(d)
         piv, _, _ = g.pivots()
         x, it = g.cg(b)
+        st = g.stats()
+    assert st["cluster_ctas"] in (8, 16)
+    assert st["cg_path_used"] == {"graph": 1, "cluster": 2}[path]
     xo, ito = ob.pcg(rp, ci, v, d, b, lp.m, lp.n, k, ob.PIVOT_GIVEN, piv, tol=1e-10, max_iter=20000)
     assert rel(x, xo) < 1e-6
     assert abs(it - ito) <= max(3, 0.05 * ito)
 
 
-def test_solve_linear_equation(case):
+@pytest.mark.parametrize("path", ["graph", "cluster"])
+def test_solve_linear_equation(case, path):
     name, lp, d, rng = case
     b1 = rng.standard_normal(lp.n)
     b2 = rng.standard_normal(lp.m)
-    with backend.GpuNormalEquations(pivots=10, cg_tol=1e-12, cg_max_iter=50000) as g:
+    with backend.GpuNormalEquations(pivots=10, cg_tol=1e-12, cg_max_iter=50000, cg_path=path) as g:
         g.LinearEquation_Construct(lp)
         g.RenewLinearEquation(d)
         x1, x2 = g.SolveLinearEquation(d, b1, b2)
@@ -115,12 +120,13 @@ def test_solve_linear_equation(case):
     assert rel(x1, ox1) < 1e-6
 
 
-def test_mixed_precision_solve(case):
+@pytest.mark.parametrize("path", ["graph", "cluster"])
+def test_mixed_precision_solve(case, path):
     name, lp, d, rng = case
     b1 = rng.standard_normal(lp.n)
     b2 = rng.standard_normal(lp.m)
     with backend.GpuNormalEquations(pivots=16, precision="mixed", ir_tol=1e-10, inner_tol=1e-4,
-                                    cg_tol=1e-14) as g:
+                                    cg_tol=1e-14, cg_path=path) as g:
         g.LinearEquation_Construct(lp)
         g.RenewLinearEquation(d)
         x1, x2 = g.SolveLinearEquation(d, b1, b2)

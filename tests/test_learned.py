@@ -1,0 +1,79 @@
+"""Ablation of the learned part on held-out multicommodity-flow LPs.
+
+Trains the MLP with the library's kernels on the IPM iterates of a few
+seeded instances, then on held-out seeds: (1) its loss beats the predictor
+without a model (no diagonal correction, warm-start scale 1), (2) the IPM
+with the model attached reaches the same optimum as the plain PCG, and
+(3) the CG iterations of both runs are reported.
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from help_gb300 import lp as L
+
+pytestmark = pytest.mark.gpu
+
+SPEC = dict(grid=8, commodities=3, pairs=3)
+TRAIN_SEEDS = list(range(6))
+TEST_SEEDS = [100, 101]
+PIVOTS = 16
+
+
+@pytest.fixture(scope="module")
+def trained():
+    torch = pytest.importorskip("torch")
+    from help_gb300 import learned
+
+    data = [learned.targets(lp, learned.collect(lp, PIVOTS)) for lp in
+            (L.generate(L.spec_mcf(**SPEC), s) for s in TRAIN_SEEDS)]
+    train = {k: np.concatenate([d[k] for d in data]) for k in ("X", "T", "W")}
+    params, losses = learned.train(train, steps=400)
+    return params, losses
+
+
+def test_training_loss_decreases(trained):
+    params, losses = trained
+    assert np.isfinite(losses).all()
+    assert losses[-1] < 0.5 * losses[0], (losses[0], losses[-1])
+
+
+def test_held_out_loss_beats_no_model(trained):
+    torch = pytest.importorskip("torch")
+    from help_gb300 import learned
+
+    params, _ = trained
+    for s in TEST_SEEDS:
+        lp = L.generate(L.spec_mcf(**SPEC), s)
+        d = learned.targets(lp, learned.collect(lp, PIVOTS))
+        mean, scale = params[learned.native.MLP_OFF_MEAN:learned.native.MLP_OFF_SCALE], params[learned.native.MLP_OFF_SCALE:]
+        xb = torch.from_numpy(learned.normalise_bits(d["X"], mean, scale).view(np.int16)).cuda()
+        m = learned.Mlp(0, params)
+        loss, _ = m.loss_grad(xb, torch.from_numpy(d["T"]).cuda(), torch.from_numpy(d["W"]).cuda(), len(d["X"]))
+        m.close()
+        base = np.array([0.0, 1.0], np.float32)
+        base_loss = float(np.sum(d["W"] * (base - d["T"]) ** 2) / np.sum(d["W"]))
+        assert loss < base_loss, (s, loss, base_loss)
+
+
+def test_ipm_with_model_matches_plain(trained):
+    from help_gb300 import learned
+
+    params, _ = trained
+    report = []
+    for s in TEST_SEEDS:
+        lp = L.generate(L.spec_mcf(**SPEC), s)
+        plain = learned.evaluate(lp, PIVOTS, None)
+        with_model = learned.evaluate(lp, PIVOTS, params)
+        assert plain["status"] == 0 and with_model["status"] == 0
+        rel = abs(plain["primal_obj"] - with_model["primal_obj"]) / abs(plain["primal_obj"])
+        assert rel < 1e-6, (s, plain["primal_obj"], with_model["primal_obj"])
+        report.append({"seed": s, "plain": plain, "learned": with_model})
+    out = os.environ.get("HELP_LEARNED_REPORT")
+    if out:
+        with open(out, "w") as f:
+            json.dump(report, f, indent=1)
+    print(json.dumps([{"seed": r["seed"], "cg_plain": r["plain"]["cg_iterations"],
+                       "cg_learned": r["learned"]["cg_iterations"]} for r in report]))
