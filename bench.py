@@ -13,10 +13,12 @@ Also reported on the same line: the FP32 product (mixed precision), the
 end-to-end product through the C ABI with host buffers, the CPU baseline
 (the reference's CSRMV_T / scale / CSRMV_N loops restated in oracle/, one
 core), the IPM time to a 1e-8 relative gap on the 2,000 x 6,000 LP (GPU,
-plain FP64 PCG), the live roofline of the dominant kernel and the SM clocks
-sampled during the timed region.
+plain FP64 PCG), the learned part's ablation on held-out multicommodity-flow
+LPs, the same product on the 104M-nonzero block-angular LP, the live
+roofline of the dominant kernel and the SM clocks sampled during the timed
+region.
 
-    python bench.py [--steps K] [--warmup W] [--gpus N] [--impl ours|reference]
+    python bench.py [--steps K] [--warmup W] [--gpus N] [--impl ours|reference] [--no-ipm] [--no-large]
 """
 from __future__ import annotations
 
@@ -150,10 +152,80 @@ def ipm_time(config: int = 0) -> dict:
         r = hsd.solve_lp(lp, g.ne_backend())
         wall = time.perf_counter() - t0
         st = g.stats()
-    return {"config": "config %d: m=%d n=%d nnz=%d" % (config, lp.m, lp.n, lp.nnz), "form": "plain FP64 PCG, k=%d, cg_tol 1e-10"
-            % L.config_pivots(config), "seconds": round(wall, 3), "status": r["status"], "iterations": r["iterations"],
+    return {"config": "config %d: m=%d n=%d nnz=%d" % (config, lp.m, lp.n, lp.nnz),
+            "form": "plain FP64 PCG, k=%d, cg_tol 1e-10, CG path %s" % (
+                L.config_pivots(config), {1: "graph", 2: "single cluster"}.get(int(st["cg_path_used"]), "?")),
+            "seconds": round(wall, 3), "status": r["status"], "iterations": r["iterations"],
             "rel_gap": r["rel_gap"], "primal_obj": r["primal_obj"], "cg_iterations": int(st["cg_iterations_total"]),
             "backend_seconds": round(r["backend_s"], 3)}
+
+
+def spmv_large(steps: int, warmup: int, local: int) -> dict:
+    """(A D^-1 A^T) v on the block-angular LP of 1,924,000 x 8,000,000 with
+    ~104M nonzeros (32 blocks + 4,000 linking rows): 2.8 GB of algorithmic
+    traffic per FP64 product, where launch costs no longer matter."""
+    import torch
+
+    from help_gb300 import backend, lp as L
+
+    lp = L.make_lp(4, 0)
+    m, n, nnz = lp.m, lp.n, lp.nnz
+    rng = np.random.default_rng(4)
+    d = np.exp(rng.uniform(np.log(1e-8), np.log(1e8), n))
+    dev = torch.device("cuda", local)
+    out = {"workload": "config 4: m=%d n=%d nnz=%d, d log-uniform [1e-8,1e8]" % (m, n, nnz)}
+    with backend.GpuNormalEquations(pivots=1, precision="mixed", device=local) as g:
+        g.LinearEquation_Construct(lp)
+        del lp
+        g.RenewLinearEquation(d)
+        for prec, dt in (("f64", torch.float64), ("f32", torch.float32)):
+            x = torch.randn(m, dtype=dt, device=dev)
+            t = torch.empty(n, dtype=dt, device=dev)
+            y = torch.empty(m, dtype=dt, device=dev)
+            fp32 = prec == "f32"
+            evs = []
+            for it in range(warmup + steps):
+                e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+                e0.record()
+                g.matvec_dev("BT", x.data_ptr(), t.data_ptr(), fp32=fp32)
+                e1.record()
+                g.matvec_dev("B", t.data_ptr(), y.data_ptr(), fp32=fp32)
+                e2.record()
+                if it >= warmup:
+                    evs.append((e0, e1, e2))
+            torch.cuda.synchronize()
+            ab = alg_bytes(m, n, nnz, 8 if prec == "f64" else 4)
+            bt = sum(a.elapsed_time(b) for a, b, _ in evs) / len(evs)
+            bb = sum(b.elapsed_time(c) for _, b, c in evs) / len(evs)
+            out[prec] = {"value": round(ab["step"] / ((bt + bb) * 1e-3) / 1e9, 1), "unit": "GB/s",
+                         "ms_per_step": round(bt + bb, 4),
+                         "passes_gbs": {"BT": round(ab["BT"] / (bt * 1e-3) / 1e9, 1),
+                                        "B": round(ab["B"] / (bb * 1e-3) / 1e9, 1)}}
+    return out
+
+
+def learned_ablation() -> dict:
+    """The learned warm start / Schur-diagonal correction trained on the IPM
+    iterates of 6 seeded multicommodity-flow LPs (8 x 8 grid, 3 commodities),
+    measured on 2 held-out seeds against the plain FP64 PCG."""
+    from help_gb300 import learned, lp as L
+
+    spec = dict(grid=8, commodities=3, pairs=3)
+    data = [learned.targets(lp, learned.collect(lp, 16)) for lp in (L.generate(L.spec_mcf(**spec), s) for s in range(6))]
+    train = {k: np.concatenate([d[k] for d in data]) for k in ("X", "T", "W")}
+    t0 = time.perf_counter()
+    params, losses = learned.train(train, steps=400)
+    train_s = time.perf_counter() - t0
+    runs = []
+    for s in (100, 101):
+        lp = L.generate(L.spec_mcf(**spec), s)
+        a, b = learned.evaluate(lp, 16, None), learned.evaluate(lp, 16, params)
+        runs.append({"seed": s, "cg_plain": a["cg_iterations"], "cg_learned": b["cg_iterations"],
+                     "s_plain": round(a["seconds"], 3), "s_learned": round(b["seconds"], 3),
+                     "obj_rel_diff": abs(a["primal_obj"] - b["primal_obj"]) / abs(a["primal_obj"]),
+                     "fallbacks": b["learned_fallbacks"]})
+    return {"train_rows": int(train["X"].shape[0]), "train_steps": 400, "train_seconds": round(train_s, 2),
+            "loss_first": losses[0], "loss_last": losses[-1], "held_out": runs}
 
 
 def run_reference(args) -> None:
@@ -200,7 +272,8 @@ def main() -> None:
     ap.add_argument("--steps", type=int, default=30)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--no-ipm", action="store_true", help="skip the IPM-time measurement")
+    ap.add_argument("--no-ipm", action="store_true", help="skip the IPM-time and learned-part measurements")
+    ap.add_argument("--no-large", action="store_true", help="skip the 104M-nonzero SpMV measurement")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
@@ -312,7 +385,16 @@ def main() -> None:
                 extra["ipm"] = ipm_time(0)
             except Exception as e:  # reported, not fatal for the kernel line
                 extra["ipm"] = {"error": str(e)}
+            try:
+                extra["learned"] = learned_ablation()
+            except Exception as e:
+                extra["learned"] = {"error": str(e)}
     g.close()
+    if rank == 0 and not args.no_large:
+        try:
+            extra["spmv_large"] = spmv_large(max(3, args.steps // 3), 2, local)
+        except Exception as e:
+            extra["spmv_large"] = {"error": str(e)}
 
     if rank == 0:
         out = {
