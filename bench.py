@@ -120,6 +120,18 @@ def dist_env():
     return ws, rank, local
 
 
+def replica_value(step_ms: float, bytes_per_step: int, ws: int, dev) -> tuple[float, float]:
+    """Replicas (one independent product per rank): the slowest rank's step
+    time, and the bytes of all ranks over it in GB/s."""
+    if ws > 1:
+        import torch
+
+        tt = torch.tensor([step_ms], dtype=torch.float64, device=dev)
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        step_ms = float(tt.item())
+    return step_ms, ws * bytes_per_step / (step_ms * 1e-3) / 1e9
+
+
 def cpu_adat_baseline(lp, d, seconds: float = 10.0) -> dict:
     """The reference's own loops for one (A D^-1 A^T) v (PCG.cpp:346-358 with
     CSRMV_T / CSRMV_N of Helper.cpp:57-81), restated in oracle/, one core."""
@@ -345,12 +357,7 @@ def main() -> None:
     # here: FP32 and FP64 agree)
     ab64 = alg_bytes(m, n, nnz, 8)
     ab32 = alg_bytes(m, n, nnz, 4)
-    step_ms = res["f64"]["step_ms"]
-    if ws > 1:
-        tt = torch.tensor([step_ms], dtype=torch.float64, device=dev)
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        step_ms = float(tt.item())
-    value = ws * ab64["step"] / (step_ms * 1e-3) / 1e9
+    step_ms, value = replica_value(res["f64"]["step_ms"], ab64["step"], ws, dev)
 
     pk = peaks()
     dom = "B" if res["f64"]["b_ms"] >= res["f64"]["bt_ms"] else "BT"
