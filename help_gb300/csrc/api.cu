@@ -51,8 +51,8 @@ double now_ms() {
 
 DevCtrl* ctrl_of(help_pcg* ctx) { return ctx->ctrl.as<DevCtrl>(); }
 
-int upload_split(help_pcg* ctx, RowSplit& S, const int32_t* ptr, int32_t rows, int g_min) {
-    RowPlanHost h = plan_rows(ptr, rows, g_min);
+int upload_split(help_pcg* ctx, RowSplit& S, const int32_t* ptr, int32_t rows, int g_min, int per_lane) {
+    RowPlanHost h = plan_rows(ptr, rows, g_min, per_lane);
     S.G = h.G;
     S.short_max = h.short_max;
     S.n_med = (int32_t)h.med.size();
@@ -67,8 +67,8 @@ int upload_split(help_pcg* ctx, RowSplit& S, const int32_t* ptr, int32_t rows, i
 
 int upload_plan(help_pcg* ctx, RowPlan& P, const int32_t* ptr, int32_t rows, bool with_f32) {
     P.rows = rows;
-    int rc = upload_split(ctx, P.s64, ptr, rows, kGminF64);
-    if (!rc && with_f32) rc = upload_split(ctx, P.s32, ptr, rows, kGminF32);
+    int rc = upload_split(ctx, P.s64, ptr, rows, kGminF64, kPerLaneF64);
+    if (!rc && with_f32) rc = upload_split(ctx, P.s32, ptr, rows, kGminF32, kPerLaneF32);
     return rc;
 }
 

@@ -49,8 +49,15 @@ struct RowPlan {
     RowSplit s64, s32;
 };
 
-constexpr int kGminF64 = 2;  // 2 lanes x 8 B = a 16-byte run per load, sector reuse through L1
-constexpr int kGminF32 = 8;  // 8 lanes x 4 B = one 32-byte sector per load
+// Lanes per short row (spmv.cuh): at least kGmin*, grown until each lane has
+// at most kPerLane* nonzeros of an average row.  Measured on GB300 (config 1,
+// 2 and 4 passes): FP32 is fastest at ~4 per lane down to groups of 2 (the
+// FP32 pass over 6-nonzero rows 74 -> 45 us against a floor of 8 lanes);
+// FP64 at ~8 per lane (its shuffle adds go through the slow FP64 pipe).
+constexpr int kGminF64 = 2;
+constexpr int kPerLaneF64 = 8;
+constexpr int kGminF32 = 2;
+constexpr int kPerLaneF32 = 4;
 
 constexpr int kTopkBins = 256;
 constexpr int kGraphIters = 8;    // CG iterations per graph launch

@@ -14,7 +14,7 @@ struct RowPlanHost {
 
 constexpr int32_t kLongRowMin = 4096;  // rows above this length take a whole CTA
 
-// g_min: smallest group (so one group's loads span a 32-byte sector).
-RowPlanHost plan_rows(const int32_t* ptr, int32_t rows, int32_t g_min);
+// g_min: smallest group; per_lane: target nonzeros per lane of an average row.
+RowPlanHost plan_rows(const int32_t* ptr, int32_t rows, int32_t g_min, int32_t per_lane);
 
 }  // namespace help

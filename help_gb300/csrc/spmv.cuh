@@ -7,9 +7,8 @@
 // Rows are split by length when the matrix is planned (host, once per matrix
 // and precision; see items.cpp):
 //   * short rows (len <= short_max = 32 G): a group of G lanes per row, G a
-//     power of two chosen so each lane handles ~4-8 nonzeros, with a floor
-//     that makes one group's loads span a whole 32-byte sector (G >= 2 for
-//     FP64, >= 8 for FP32).  A warp covers 32 / G consecutive rows, so its
+//     power of two (at least 2) chosen so each lane handles ~8 (FP64) or ~4
+//     (FP32) nonzeros of an average row.  A warp covers 32 / G consecutive rows, so its
 //     loads sweep one contiguous span of the value and index arrays; each lane
 //     keeps one FMA accumulator and the group combines with log2(G) shuffles;
 //   * medium rows (short_max < len <= kLongRowMin): one warp per row;
