@@ -14,11 +14,13 @@ end-to-end product through the C ABI with host buffers, the CPU baseline
 (the reference's CSRMV_T / scale / CSRMV_N loops restated in oracle/, one
 core), the IPM time to a 1e-8 relative gap on the 2,000 x 6,000 LP (GPU,
 plain FP64 PCG), the learned part's ablation on held-out multicommodity-flow
-LPs, the same product on the 104M-nonzero block-angular LP, the live
+LPs, PCG iterations per second (configs 0 and 1 by default), the same
+product on the 104M-nonzero block-angular LP, the live
 roofline of the dominant kernel and the SM clocks sampled during the timed
 region.
 
     python bench.py [--steps K] [--warmup W] [--gpus N] [--impl ours|reference] [--no-ipm] [--no-large]
+                    [--pcg-configs 0,1] [--pcg-iters I] [--pcg-only]
 """
 from __future__ import annotations
 
@@ -216,6 +218,31 @@ def spmv_large(steps: int, warmup: int, local: int) -> dict:
     return out
 
 
+def pcg_rate(config: int, iters: int, local: int) -> dict:
+    """PCG iterations per second (FP64) on the given configuration with its
+    pivot count, d log-uniform in [1e-8, 1e8]: one CG run of exactly `iters`
+    iterations (unreachable tolerance), timed on the device with CUDA events."""
+    from help_gb300 import backend, lp as L
+
+    lp = L.make_lp(config, 0)
+    rng = np.random.default_rng(7)
+    d = np.exp(rng.uniform(np.log(1e-8), np.log(1e8), lp.n))
+    b = rng.standard_normal(lp.m)
+    k = L.config_pivots(config)
+    with backend.GpuNormalEquations(pivots=k, cg_tol=1e-300, cg_max_iter=iters, device=local) as g:
+        g.LinearEquation_Construct(lp)
+        g.RenewLinearEquation(d)
+        renew_ms = g.stats()["renew_ms"]
+        g.cg(b)  # graph capture and warm-up
+        _, it = g.cg(b)
+        st = g.stats()
+    us = st["cg_kernel_ms"] * 1e3 / max(it, 1)
+    return {"workload": "config %d: m=%d n=%d nnz=%d, k=%d, nnz(C)=%d" % (config, lp.m, lp.n, lp.nnz, k, st["nnz_c"]),
+            "iterations": int(it), "us_per_iteration": round(us, 2), "iterations_per_s": round(1e6 / us, 1),
+            "renew_ms": round(renew_ms, 2),
+            "path": {1: "graph", 2: "single cluster"}.get(int(st["cg_path_used"]), "?")}
+
+
 def learned_ablation() -> dict:
     """The learned warm start / Schur-diagonal correction trained on the IPM
     iterates of 6 seeded multicommodity-flow LPs (8 x 8 grid, 3 commodities),
@@ -286,9 +313,20 @@ def main() -> None:
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-ipm", action="store_true", help="skip the IPM-time and learned-part measurements")
     ap.add_argument("--no-large", action="store_true", help="skip the 104M-nonzero SpMV measurement")
+    ap.add_argument("--pcg-configs", default="0,1", help="configurations whose PCG iteration rate is measured")
+    ap.add_argument("--pcg-iters", type=int, default=500, help="CG iterations per rate measurement")
+    ap.add_argument("--pcg-only", action="store_true", help="only the PCG iteration rates (profiling runs)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
+        return
+    if args.pcg_only:
+        import torch
+
+        ws, rank, local = dist_env()
+        torch.cuda.set_device(local)
+        out = {c: pcg_rate(int(c), args.pcg_iters, local) for c in args.pcg_configs.split(",") if c}
+        print(json.dumps({"pcg": out}), flush=True)
         return
 
     import torch
@@ -397,6 +435,13 @@ def main() -> None:
             except Exception as e:
                 extra["learned"] = {"error": str(e)}
     g.close()
+    if rank == 0:
+        extra["pcg"] = {}
+        for c in [int(v) for v in args.pcg_configs.split(",") if v]:
+            try:
+                extra["pcg"]["config%d" % c] = pcg_rate(c, args.pcg_iters, local)
+            except Exception as e:
+                extra["pcg"]["config%d" % c] = {"error": str(e)}
     if rank == 0 and not args.no_large:
         try:
             extra["spmv_large"] = spmv_large(max(3, args.steps // 3), 2, local)

@@ -1012,9 +1012,15 @@ int help_pcg_cg(help_pcg* ctx, const double* b, double* x, int64_t* iters) {
     if (rc) return rc;
     CK(vec_fill(ctx->x.as<double>(), 0.0, ctx->m, ctx->stream));
     CgResult res;
+    ctx->solve_kernel_ms = 0;
+    ctx->solve_launches = 0;
     rc = run_pcg<double>(ctx, ctx->x.as<double>(), ctx->r0.as<double>(), ctx->opt.cg_tol, ctx->opt.cg_max_iter, 0, &res);
     if (rc) return rc;
     if (iters) *iters = res.iterations;
+    // device time of this CG run, for iteration-rate measurements
+    ctx->stats.cg_iterations = res.iterations;
+    ctx->stats.cg_kernel_ms = ctx->solve_kernel_ms;
+    ctx->stats.cg_launches = ctx->solve_launches;
     return d2h(ctx, x, ctx->x.as<double>(), ctx->m);
 }
 

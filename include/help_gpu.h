@@ -143,7 +143,8 @@ int help_pcg_precond_apply(help_pcg* ctx, const double* r, double* z);
  * D_S used for non-pivot rows (PCG.cpp:41-46, :100-102). Any pointer may be NULL. */
 int help_pcg_get_pivots(help_pcg* ctx, int32_t* pivots, double* diag_g, double* diag_s);
 /* One PCG run on (A D^-1 A^T + delta I) x = b from x = 0 with the current
- * preconditioner (ConjugateGradient, PCG.cpp:296-395); returns iterations in *iters. */
+ * preconditioner (ConjugateGradient, PCG.cpp:296-395); returns iterations in
+ * *iters; stats cg_iterations / cg_kernel_ms / cg_launches describe this run. */
 int help_pcg_cg(help_pcg* ctx, const double* b, double* x, int64_t* iters);
 
 /* Explicit A diag(w) A^T, upper triangle incl. diagonal, CSR with columns
