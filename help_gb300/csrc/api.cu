@@ -57,10 +57,23 @@ int upload_split(help_pcg* ctx, RowSplit& S, const int32_t* ptr, int32_t rows, i
     S.short_max = h.short_max;
     S.n_med = (int32_t)h.med.size();
     S.n_long = (int32_t)h.lng.size();
+    S.n_seg = (int32_t)(h.seg.size() / 4);
     CK(S.med.ensure(4 * std::max<size_t>(h.med.size(), 1)));
     CK(S.lng.ensure(4 * std::max<size_t>(h.lng.size(), 1)));
+    CK(S.seg.ensure(4 * std::max<size_t>(h.seg.size(), 4)));
+    CK(S.lnseg.ensure(4 * std::max<size_t>(h.lng.size(), 1)));
+    CK(S.lbase.ensure(4 * std::max<size_t>(h.lng.size(), 1)));
+    CK(S.tickets.ensure(4 * std::max<size_t>(h.lng.size(), 1)));
+    CK(S.parts.ensure(8 * std::max<size_t>((size_t)h.n_parts, 1)));
     if (!h.med.empty()) CK(cudaMemcpyAsync(S.med.p, h.med.data(), 4 * h.med.size(), cudaMemcpyHostToDevice, ctx->stream));
-    if (!h.lng.empty()) CK(cudaMemcpyAsync(S.lng.p, h.lng.data(), 4 * h.lng.size(), cudaMemcpyHostToDevice, ctx->stream));
+    if (!h.lng.empty()) {
+        CK(cudaMemcpyAsync(S.lng.p, h.lng.data(), 4 * h.lng.size(), cudaMemcpyHostToDevice, ctx->stream));
+        CK(cudaMemcpyAsync(S.seg.p, h.seg.data(), 4 * h.seg.size(), cudaMemcpyHostToDevice, ctx->stream));
+        CK(cudaMemcpyAsync(S.lnseg.p, h.long_nseg.data(), 4 * h.lng.size(), cudaMemcpyHostToDevice, ctx->stream));
+        CK(cudaMemcpyAsync(S.lbase.p, h.long_base.data(), 4 * h.lng.size(), cudaMemcpyHostToDevice, ctx->stream));
+        // the last CTA of a row resets its ticket, so zero once here
+        CK(cudaMemsetAsync(S.tickets.p, 0, 4 * h.lng.size(), ctx->stream));
+    }
     CK(cudaStreamSynchronize(ctx->stream));  // h goes out of scope
     return HELP_OK;
 }
@@ -86,6 +99,12 @@ SpmvView<V> view(const RowPlan& P, const DevMem& ptr, const DevMem& idx, const D
     v.val = val.as<V>();
     v.med_rows = S.med.as<int>();
     v.long_rows = S.lng.as<int>();
+    v.n_seg = S.n_seg;
+    v.segs = S.seg.as<int4>();
+    v.long_nseg = S.lnseg.as<int>();
+    v.long_base = S.lbase.as<int>();
+    v.tickets = S.tickets.as<unsigned int>();
+    v.parts = S.parts.as<double>();
     return v;
 }
 
@@ -428,9 +447,8 @@ void release_all(help_pcg* ctx) {
     RowPlan* plans[] = {&ctx->pl_csr, &ctx->pl_csc, &ctx->pl_c, &ctx->pl_ct};
     for (RowPlan* p : plans) {
         for (RowSplit* s : {&p->s64, &p->s32}) {
-            s->med.release();
-            s->lng.release();
-            s->n_med = s->n_long = 0;
+            for (DevMem* d : {&s->med, &s->lng, &s->seg, &s->lnseg, &s->lbase, &s->tickets, &s->parts}) d->release();
+            s->n_med = s->n_long = s->n_seg = 0;
         }
         p->rows = 0;
     }

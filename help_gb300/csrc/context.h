@@ -42,7 +42,8 @@ struct DevMem {
 // per precision (the group-size floor differs).
 struct RowSplit {
     DevMem med, lng;
-    int32_t G = 1, short_max = 32, n_med = 0, n_long = 0;
+    DevMem seg, lnseg, lbase, tickets, parts;  // segments of long rows (items.h)
+    int32_t G = 1, short_max = 32, n_med = 0, n_long = 0, n_seg = 0;
 };
 struct RowPlan {
     int32_t rows = 0;

@@ -10,9 +10,16 @@ struct RowPlanHost {
     int32_t G = 1;          // lanes per short row
     int32_t short_max = 32; // longer rows are medium or long
     std::vector<int32_t> med, lng;
+    // long rows cut into segments of at most kSegLen nonzeros, one CTA each:
+    // seg = {row, begin, end, long-row index j}; row j's partial sums go to
+    // slots long_base[j] .. long_base[j] + long_nseg[j] - 1
+    std::vector<int32_t> seg;  // 4 ints per segment
+    std::vector<int32_t> long_nseg, long_base;
+    int32_t n_parts = 0;
 };
 
-constexpr int32_t kLongRowMin = 4096;  // rows above this length take a whole CTA
+constexpr int32_t kLongRowMin = 4096;  // rows above this length are long
+constexpr int32_t kSegLen = 16384;     // nonzeros per segment of a long row (one CTA)
 
 // g_min: smallest group; per_lane: target nonzeros per lane of an average row.
 RowPlanHost plan_rows(const int32_t* ptr, int32_t rows, int32_t g_min, int32_t per_lane);

@@ -136,30 +136,42 @@ __global__ void __launch_bounds__(kCgThreads) k_p2(const CgArgs<V> A) {
                 rz = fma((double)ri, (double)zi, rz);
             }
         },
+        [&](int i, V s) {  // long rows: their r.z terms are added by k_p3's last block
+            if (A.pivpos[i] < 0) A.z[i] = A.dsinv[i] * (r[i] - s);
+        },
         red);
     rz = block_sum(rz, red);
     if (threadIdx.x == 0) A.part_rz[blockIdx.x] = rz;
 }
 
-// ---- P3: w = r_P - C^T z_N, partial a . w; last block: rz, beta
+// Fixed-order sum over the long rows of M of term(row), by the calling block.
+template <class V, class T>
+HELP_DEVINL double long_rows_sum(const SpmvView<V>& M, const T& term, double* red) {
+    double s = 0.0;
+    for (int j = threadIdx.x; j < M.n_long; j += blockDim.x) s += term(M.long_rows[j]);
+    return block_sum(s, red);
+}
+
+// ---- P3: w = r_P - C^T z_N; last block: rz = r_N.z_N + a.w, beta
 template <class V>
 __global__ void __launch_bounds__(kCgThreads) k_p3(const CgArgs<V> A) {
     if (cg_done(A.sc)) return;
     __shared__ double red[kCgThreads];
     const V* r = (A.sc->it & 1) ? A.r1 : A.r0;
-    double aw = 0.0;
     spmv_rows<V>(
         A.ct, [&](int i) { return A.z[i]; },
-        [&](int c, V s) {
-            const double wc = (double)r[A.piv[c]] - (double)s;
-            A.w[c] = wc;
-            aw = fma(A.a[c], wc, aw);
-        },
-        red);
-    aw = block_sum(aw, red);
-    if (publish_partial(aw, A.part_aw, &A.sc->ticket[1])) {
-        // k_p2 ran with the same grid, so part_rz holds gridDim.x partials too
-        const double rz = sum_parts(A.part_rz, A.part_aw, gridDim.x, red);
+        [&](int c, V s) { A.w[c] = (double)r[A.piv[c]] - (double)s; }, red);
+    if (publish_partial(0.0, A.part_aw, &A.sc->ticket[1])) {
+        // every block has written its w entries: r_P . z_P = a . w over all k
+        // in order, plus the r.z terms of C's long rows, plus k_p2's partials
+        // (same grid)
+        double aw = 0.0;
+        for (int c = threadIdx.x; c < A.k; c += blockDim.x) aw = fma(A.a[c], __ldcg(A.w + c), aw);
+        aw = block_sum(aw, red);
+        const double rzl = long_rows_sum(
+            A.c,
+            [&](int i) { return A.pivpos[i] < 0 ? (double)__ldcg(r + i) * (double)__ldcg(A.z + i) : 0.0; }, red);
+        const double rz = sum_parts(A.part_rz, nullptr, gridDim.x, red) + rzl + aw;
         if (threadIdx.x == 0) {
             CgScalars* sc = A.sc;
             sc->ticket[1] = 0;
@@ -226,10 +238,12 @@ __global__ void __launch_bounds__(kCgThreads) k_b(const CgArgs<V> A) {
             A.q[i] = qi;
             pq = fma((double)pi, (double)qi, pq);
         },
-        red);
+        [&](int i, V s) { A.q[i] = has_delta ? fma_t(vd, pn[i], s) : s; }, red);
     pq = block_sum(pq, red);
     if (publish_partial(pq, A.part_pq, &A.sc->ticket[2])) {
-        const double tot = sum_parts(A.part_pq, nullptr, gridDim.x, red);
+        const double pql = long_rows_sum(
+            A.csr, [&](int i) { return (double)__ldcg(pn + i) * (double)__ldcg(A.q + i); }, red);
+        const double tot = sum_parts(A.part_pq, nullptr, gridDim.x, red) + pql;
         if (threadIdx.x == 0) {
             CgScalars* sc = A.sc;
             sc->ticket[2] = 0;
@@ -371,24 +385,29 @@ __global__ void __launch_bounds__(kClusterThreads) k_cg_cluster(const CgArgs<V> 
                     prz = fma((double)ri, (double)zi, prz);
                 }
             },
+            [&](int i, V s) {
+                if (A.pivpos[i] < 0) A.z[i] = A.dsinv[i] * (__ldcg(r + i) - s);
+            },
             red);
         prz = block_sum(prz, red);
         if (tid == 0) s_part[0] = prz;
         cl.sync();
         // P3: w = r_P - C^T z_N
-        double paw = 0.0;
         spmv_rows<V>(
             A.ct, [&](int i) { return __ldcg(A.z + i); },
-            [&](int c, V s) {
-                const double wc = (double)__ldcg(r + A.piv[c]) - (double)s;
-                A.w[c] = wc;
-                paw = fma(__ldcg(A.a + c), wc, paw);
-            },
-            red);
-        paw = block_sum(paw, red);
-        if (tid == 0) s_part[1] = paw;
+            [&](int c, V s) { A.w[c] = (double)__ldcg(r + A.piv[c]) - (double)s; }, red);
         cl.sync();
-        rz = cluster_total(cl, s_part, 0, 1, &s_tot[0]);
+        {
+            // a . w over all k and the long rows' r.z terms, the same in every CTA
+            double aw = 0.0;
+            for (int c = tid; c < A.k; c += blockDim.x) aw = fma(__ldcg(A.a + c), __ldcg(A.w + c), aw);
+            aw = block_sum(aw, red);
+            const double rzl = long_rows_sum(
+                A.c,
+                [&](int i) { return A.pivpos[i] < 0 ? (double)__ldcg(r + i) * (double)__ldcg(A.z + i) : 0.0; },
+                red);
+            rz = cluster_total(cl, s_part, 0, -1, &s_tot[0]) + rzl + aw;
+        }
         if (!(rz > 0.0)) {
             done = 3;
             break;
@@ -426,11 +445,13 @@ __global__ void __launch_bounds__(kClusterThreads) k_cg_cluster(const CgArgs<V> 
                 A.q[i] = qi;
                 ppq = fma((double)pi, (double)qi, ppq);
             },
-            red);
+            [&](int i, V s) { A.q[i] = has_delta ? fma_t(vd, __ldcg(pn + i), s) : s; }, red);
         ppq = block_sum(ppq, red);
         if (tid == 0) s_part[2] = ppq;
         cl.sync();
-        const double pq = cluster_total(cl, s_part, 2, -1, &s_tot[1]);
+        const double pql =
+            long_rows_sum(A.csr, [&](int i) { return (double)__ldcg(pn + i) * (double)__ldcg(A.q + i); }, red);
+        const double pq = cluster_total(cl, s_part, 2, -1, &s_tot[1]) + pql;
         if (!(pq > 0.0)) {
             done = 3;
             break;

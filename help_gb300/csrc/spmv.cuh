@@ -12,7 +12,11 @@
 //     loads sweep one contiguous span of the value and index arrays; each lane
 //     keeps one FMA accumulator and the group combines with log2(G) shuffles;
 //   * medium rows (short_max < len <= kLongRowMin): one warp per row;
-//   * long rows (len > kLongRowMin): one CTA per row.
+//   * long rows (len > kLongRowMin): cut into segments of kSegLen nonzeros,
+//     one CTA per segment.  Each CTA writes its segment's sum to a partial
+//     slot and takes a ticket on the row; the CTA that takes the last ticket
+//     adds the row's partials in segment order (deterministic), resets the
+//     ticket and runs the epilogue.  No CTA waits for another.
 // Loads go through L1 (read-only path) so the neighbouring elements a group
 // reads next reuse the sectors already fetched.  All loops are grid-stride
 // over every warp / block of the launch, so the same routine serves the
@@ -22,6 +26,7 @@
 #pragma once
 
 #include "common.cuh"
+#include "items.h"
 
 namespace help {
 
@@ -36,25 +41,37 @@ struct SpmvView {
     const int* idx;
     const V* val;
     const int* med_rows;   // warp-per-row
-    const int* long_rows;  // CTA-per-row
+    const int* long_rows;  // rows longer than kLongRowMin, ascending
+    // segments of the long rows (items.h): {row, begin, end, long-row index}
+    int n_seg = 0;
+    const int4* segs = nullptr;
+    const int* long_nseg = nullptr;
+    const int* long_base = nullptr;
+    unsigned int* tickets = nullptr;  // one per long row, zero between launches
+    double* parts = nullptr;          // partial sums of the segments
 };
 
 //   xf(col)  -> V     value of the dense operand at index `col`
 //   ep(row, sum)      epilogue for one finished row (called by one thread)
+//   epl(row, sum)     the same for long rows; it runs in whichever CTA
+//                     finishes the row last, so a kernel whose epilogue also
+//                     accumulates a reduction passes an epl that only stores
+//                     and adds the long rows' terms in a fixed order itself
 // red: blockDim doubles of shared memory (CTA reductions of long rows).
-template <class V, class XF, class EP>
-HELP_DEVINL void spmv_rows(const SpmvView<V>& M, const XF& xf, const EP& ep, double* red) {
+template <class V, class XF, class EP, class EPL>
+HELP_DEVINL void spmv_rows(const SpmvView<V>& M, const XF& xf, const EP& ep, const EPL& epl, double* red) {
     const int tid = threadIdx.x, nthr = blockDim.x;
     const int lane = tid & 31, warp = tid >> 5, nw = nthr >> 5;
     const int gw = blockIdx.x * nw + warp, tw = gridDim.x * nw;
     const int* __restrict__ ptr = M.ptr;
     const int* __restrict__ idx = M.idx;
     const V* __restrict__ val = M.val;
+    __shared__ int s_last;
 
-    // long rows: the whole CTA
-    for (int i = blockIdx.x; i < M.n_long; i += gridDim.x) {
-        const int r = ld_ro(M.long_rows + i);
-        const int b = ld_ro(ptr + r), e = ld_ro(ptr + r + 1);
+    // long rows: one CTA per segment
+    for (int sg = blockIdx.x; sg < M.n_seg; sg += gridDim.x) {
+        const int4 S = ld_ro(M.segs + sg);
+        const int r = S.x, b = S.y, e = S.z, j = S.w;
         V acc = V(0);
         int q = b + tid;
         for (; q + 3 * nthr < e; q += 4 * nthr) {
@@ -69,8 +86,28 @@ HELP_DEVINL void spmv_rows(const SpmvView<V>& M, const XF& xf, const EP& ep, dou
             acc = fma_t(v3, x3, acc);
         }
         for (; q < e; q += nthr) acc = fma_t(ld_ro(val + q), xf(ld_ro(idx + q)), acc);
-        const double s = block_sum((double)acc, red);
-        if (tid == 0) ep(r, (V)s);
+        const double sum = block_sum((double)acc, red);
+        const int nseg = ld_ro(M.long_nseg + j);
+        if (nseg == 1) {
+            if (tid == 0) epl(r, (V)sum);
+            continue;
+        }
+        const int base = ld_ro(M.long_base + j);
+        if (tid == 0) {
+            M.parts[base + (b - ld_ro(ptr + r)) / kSegLen] = sum;
+            __threadfence();
+            const unsigned int t = atomicAdd(M.tickets + j, 1u);
+            s_last = (t == (unsigned int)nseg - 1u);
+        }
+        __syncthreads();
+        if (s_last && tid == 0) {
+            __threadfence();
+            double tot = 0.0;
+            for (int k = 0; k < nseg; ++k) tot += __ldcg(M.parts + base + k);
+            M.tickets[j] = 0u;
+            epl(r, (V)tot);
+        }
+        __syncthreads();
     }
 
     // medium rows: one warp each
@@ -124,6 +161,11 @@ HELP_DEVINL void spmv_rows(const SpmvView<V>& M, const XF& xf, const EP& ep, dou
         for (int o = G >> 1; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
         if (mine && sub == 0) ep(r, acc);
     }
+}
+
+template <class V, class XF, class EP>
+HELP_DEVINL void spmv_rows(const SpmvView<V>& M, const XF& xf, const EP& ep, double* red) {
+    spmv_rows<V>(M, xf, ep, ep, red);
 }
 
 }  // namespace help

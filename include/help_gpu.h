@@ -14,7 +14,9 @@
  *     caller; the library keeps its own device copies of A and all scratch;
  *   - d is D = X^-1 Z itself (not inverted);
  *   - solve writes x_1 (n) and x_2 (m) in full;
- *   - single-threaded caller, no re-entrancy on one context.
+ *   - single-threaded caller, no re-entrancy on one context: calls on one
+ *     context must not overlap on the GPU either (help_pcg_matvec_dev on
+ *     two streams), as they share its scratch (long-row partial sums).
  * Every entry point returns HELP_OK (0) or a negative HELP_E* code; the
  * reference's backends exit() on fatal errors instead (Helper.cpp:24-35), the
  * UsePCG_GPU.cpp shim keeps that behaviour.

@@ -24,6 +24,9 @@ CASES = {
     "zipf": lambda: L.generate(L.spec_zipf(3000, 12000, 6, 1.3, 70), 4),
     "block": lambda: L.generate(L.spec_block(4, 300, 1200, 5, 40, 0.05), 5),
     "mcf": lambda: L.generate(L.spec_mcf(12, 3, 3), 6),
+    # 4 linking rows of ~19k nonzeros: long rows split over 2 CTAs each, and
+    # pivot columns of C with ~8k entries (long rows of C^T, one CTA each)
+    "longrows": lambda: L.generate(L.spec_block(8, 1000, 4000, 5, 4, 0.6), 8),
 }
 
 
@@ -141,9 +144,17 @@ def test_mixed_precision_solve(case, path):
 def test_adat_assembly_bitwise(case):
     name, lp, d, rng = case
     rp, ci, v = lp.csr()
-    if name == "zipf":
-        pytest.skip("rows beyond the explicit assembly's per-row capacity")
     w = np.exp(rng.uniform(-2, 2, lp.n))
+    if name in ("zipf", "longrows"):
+        # rows with more contributions than the assembly's per-row capacity:
+        # a clean error, and the context stays usable
+        with backend.GpuNormalEquations(pivots=1) as g:
+            g.LinearEquation_Construct(lp)
+            with pytest.raises(backend.BackendError, match="more contributions"):
+                g.adat(w)
+            x = rng.standard_normal(lp.n)
+            assert rel(g.matvec("A", x), ob.csrmv_n(rp, ci, v, x, lp.m, lp.n)) < 1e-13
+        return
     with backend.GpuNormalEquations(pivots=1) as g:
         g.LinearEquation_Construct(lp)
         grp, gcol, gval = g.adat(w)
@@ -179,3 +190,31 @@ def test_bad_d_is_an_error():
             g.RenewLinearEquation(d)
         g.RenewLinearEquation(np.ones(lp.n))          # context still usable afterwards
         assert g.stats()["pivots"] == 4
+
+
+def test_long_rows_repeatable_and_fp32():
+    """Rows split over several CTAs give bitwise the same product on every
+    call (partials added in segment order, tickets reset by the last CTA),
+    in FP64 and in the FP32 copy, and FP32 agrees with FP64 to 1e-5."""
+    torch = pytest.importorskip("torch")
+    lp = CASES["longrows"]()
+    rng = np.random.default_rng(12)
+    d = np.exp(rng.uniform(-6, 6, lp.n))
+    rp, ci, v = lp.csr()
+    with backend.GpuNormalEquations(pivots=4, precision="mixed") as g:
+        g.LinearEquation_Construct(lp)
+        g.RenewLinearEquation(d)
+        w = rng.standard_normal(lp.m)
+        y1, y2 = g.matvec("ADAT", w), g.matvec("ADAT", w)
+        assert np.array_equal(y1, y2)
+        t = ob.csrmv_t(rp, ci, v, w, lp.m, lp.n) / d
+        assert rel(y1, ob.csrmv_n(rp, ci, v, t, lp.m, lp.n)) < 1e-11
+        x32 = torch.from_numpy(w.astype(np.float32)).cuda()
+        outs = []
+        for _ in range(2):
+            y32 = torch.empty(lp.m, dtype=torch.float32, device="cuda")
+            g.matvec_dev("ADAT", x32.data_ptr(), y32.data_ptr(), fp32=True)
+            torch.cuda.synchronize()
+            outs.append(y32.cpu().numpy().astype(np.float64))
+        assert np.array_equal(outs[0], outs[1])
+        assert rel(outs[0], y1) < 1e-5
