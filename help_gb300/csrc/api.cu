@@ -58,6 +58,12 @@ int upload_split(help_pcg* ctx, RowSplit& S, const int32_t* ptr, int32_t rows, i
     S.n_med = (int32_t)h.med.size();
     S.n_long = (int32_t)h.lng.size();
     S.n_seg = (int32_t)(h.seg.size() / 4);
+    S.n_short = (int32_t)h.short_order.size();
+    if (S.n_short > 0) {
+        CK(S.sorder.ensure(4 * (size_t)S.n_short));
+        CK(cudaMemcpyAsync(S.sorder.p, h.short_order.data(), 4 * (size_t)S.n_short, cudaMemcpyHostToDevice,
+                           ctx->stream));
+    }
     CK(S.med.ensure(4 * std::max<size_t>(h.med.size(), 1)));
     CK(S.lng.ensure(4 * std::max<size_t>(h.lng.size(), 1)));
     CK(S.seg.ensure(4 * std::max<size_t>(h.seg.size(), 4)));
@@ -105,6 +111,8 @@ SpmvView<V> view(const RowPlan& P, const DevMem& ptr, const DevMem& idx, const D
     v.long_base = S.lbase.as<int>();
     v.tickets = S.tickets.as<unsigned int>();
     v.parts = S.parts.as<double>();
+    v.short_order = S.n_short > 0 ? S.sorder.as<int>() : nullptr;
+    v.n_short = S.n_short;
     return v;
 }
 
@@ -447,8 +455,9 @@ void release_all(help_pcg* ctx) {
     RowPlan* plans[] = {&ctx->pl_csr, &ctx->pl_csc, &ctx->pl_c, &ctx->pl_ct};
     for (RowPlan* p : plans) {
         for (RowSplit* s : {&p->s64, &p->s32}) {
-            for (DevMem* d : {&s->med, &s->lng, &s->seg, &s->lnseg, &s->lbase, &s->tickets, &s->parts}) d->release();
-            s->n_med = s->n_long = s->n_seg = 0;
+            for (DevMem* d : {&s->med, &s->lng, &s->seg, &s->lnseg, &s->lbase, &s->tickets, &s->parts, &s->sorder})
+                d->release();
+            s->n_med = s->n_long = s->n_seg = s->n_short = 0;
         }
         p->rows = 0;
     }

@@ -43,7 +43,8 @@ struct DevMem {
 struct RowSplit {
     DevMem med, lng;
     DevMem seg, lnseg, lbase, tickets, parts;  // segments of long rows (items.h)
-    int32_t G = 1, short_max = 32, n_med = 0, n_long = 0, n_seg = 0;
+    DevMem sorder;                             // short rows in processing order (when uneven)
+    int32_t G = 1, short_max = 32, n_med = 0, n_long = 0, n_seg = 0, n_short = 0;
 };
 struct RowPlan {
     int32_t rows = 0;

@@ -7,7 +7,17 @@
 // nonzeros, one CTA per segment, so one row of 250k nonzeros (a pivot column
 // of a Zipf matrix's Schur block) does not hold a whole launch behind one CTA.
 // Medium rows, long rows and segments are listed explicitly.
+//
+// A warp walks 32 / G short rows together until the longest is done, and on
+// GB300 an FP64 instruction costs its issue slots whatever lanes are active,
+// so rows of very uneven length next to each other waste the FP64 pipe (the
+// Schur block of a Zipf matrix: median row 7, some 900).  When index order
+// wastes more than kOrderWaste of the lane steps, short rows are processed by
+// decreasing length within windows of kOrderWindow consecutive rows, which
+// keeps a warp's rows' vector entries close together.
 #include "items.h"
+
+#include <algorithm>
 
 namespace help {
 
@@ -44,6 +54,42 @@ RowPlanHost plan_rows(const int32_t* ptr, int32_t rows, int32_t g_min, int32_t p
         } else if (len > p.short_max) {
             p.med.push_back(i);
         }
+    }
+    // lane steps of a warp group = rows per warp x steps of its longest row
+    const int32_t rpw = 32 / G;
+    auto steps = [&](int32_t r) -> int64_t {
+        const int32_t len = ptr[r + 1] - ptr[r];
+        return len <= p.short_max ? (len + G - 1) / G : 0;
+    };
+    int64_t useful = 0, index_cost = 0;
+    for (int32_t b = 0; b < rows; b += rpw) {
+        int64_t mx = 0;
+        for (int32_t r = b; r < std::min(rows, b + rpw); ++r) {
+            const int64_t st = steps(r);
+            useful += st;
+            mx = std::max(mx, st);
+        }
+        index_cost += mx * rpw;
+    }
+    if (useful > 0 && (double)index_cost > kOrderWaste * (double)useful) {
+        std::vector<int32_t> win;
+        for (int32_t w0 = 0; w0 < rows; w0 += kOrderWindow) {
+            win.clear();
+            for (int32_t r = w0; r < std::min(rows, w0 + kOrderWindow); ++r)
+                if (ptr[r + 1] - ptr[r] <= p.short_max) win.push_back(r);
+            std::stable_sort(win.begin(), win.end(),
+                             [&](int32_t a, int32_t b) { return ptr[a + 1] - ptr[a] > ptr[b + 1] - ptr[b]; });
+            p.short_order.insert(p.short_order.end(), win.begin(), win.end());
+        }
+        int64_t cost = 0;
+        for (size_t b = 0; b < p.short_order.size(); b += rpw) {
+            int64_t mx = 0;
+            for (size_t q = b; q < std::min(p.short_order.size(), b + rpw); ++q) mx = std::max(mx, steps(p.short_order[q]));
+            cost += mx * rpw;
+        }
+        p.warp_waste = (double)cost / (double)useful;
+    } else if (useful > 0) {
+        p.warp_waste = (double)index_cost / (double)useful;
     }
     return p;
 }

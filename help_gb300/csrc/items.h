@@ -16,10 +16,16 @@ struct RowPlanHost {
     std::vector<int32_t> seg;  // 4 ints per segment
     std::vector<int32_t> long_nseg, long_base;
     int32_t n_parts = 0;
+    // short rows in processing order when their lengths are uneven (empty:
+    // all rows in index order, non-short ones skipped)
+    std::vector<int32_t> short_order;
+    double warp_waste = 1.0;  // lane-steps of the chosen order over the useful ones
 };
 
 constexpr int32_t kLongRowMin = 4096;  // rows above this length are long
 constexpr int32_t kSegLen = 16384;     // nonzeros per segment of a long row (one CTA)
+constexpr int32_t kOrderWindow = 4096; // short rows are reordered only within windows of this many rows
+constexpr double kOrderWaste = 1.5;    // reorder when index order wastes this factor of lane steps
 
 // g_min: smallest group; per_lane: target nonzeros per lane of an average row.
 RowPlanHost plan_rows(const int32_t* ptr, int32_t rows, int32_t g_min, int32_t per_lane);

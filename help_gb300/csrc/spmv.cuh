@@ -8,9 +8,12 @@
 // and precision; see items.cpp):
 //   * short rows (len <= short_max = 32 G): a group of G lanes per row, G a
 //     power of two (at least 2) chosen so each lane handles ~8 (FP64) or ~4
-//     (FP32) nonzeros of an average row.  A warp covers 32 / G consecutive rows, so its
-//     loads sweep one contiguous span of the value and index arrays; each lane
-//     keeps one FMA accumulator and the group combines with log2(G) shuffles;
+//     (FP32) nonzeros of an average row.  A warp covers 32 / G rows -- in
+//     index order, so its loads sweep one contiguous span of the value and
+//     index arrays, or, for matrices whose row lengths vary a lot, by
+//     decreasing length within windows of consecutive rows (short_order) so a
+//     warp's rows finish together; each lane keeps one FMA accumulator and
+//     the group combines with log2(G) shuffles;
 //   * medium rows (short_max < len <= kLongRowMin): one warp per row;
 //   * long rows (len > kLongRowMin): cut into segments of kSegLen nonzeros,
 //     one CTA per segment.  Each CTA writes its segment's sum to a partial
@@ -49,6 +52,9 @@ struct SpmvView {
     const int* long_base = nullptr;
     unsigned int* tickets = nullptr;  // one per long row, zero between launches
     double* parts = nullptr;          // partial sums of the segments
+    // short rows in processing order (null: index order, non-short rows skipped)
+    const int* short_order = nullptr;
+    int n_short = 0;
 };
 
 //   xf(col)  -> V     value of the dense operand at index `col`
@@ -135,14 +141,17 @@ HELP_DEVINL void spmv_rows(const SpmvView<V>& M, const XF& xf, const EP& ep, con
     // short rows: G lanes per row, 32 / G rows per warp step
     const int G = M.G, lg = __ffs(G) - 1;
     const int sub = lane & (G - 1), rpw = 32 >> lg;
-    for (int base = gw * rpw; base < M.rows; base += tw * rpw) {
-        const int r = base + (lane >> lg);
+    const bool ordered = M.short_order != nullptr;
+    const int slots = ordered ? M.n_short : M.rows;
+    for (int base = gw * rpw; base < slots; base += tw * rpw) {
+        const int slot = base + (lane >> lg);
+        const int r = (ordered && slot < slots) ? ld_ro(M.short_order + slot) : slot;
         int b = 0, e = 0;
-        if (r < M.rows) {
+        if (slot < slots) {
             b = ld_ro(ptr + r);
             e = ld_ro(ptr + r + 1);
         }
-        const bool mine = (r < M.rows) && (e - b <= M.short_max);
+        const bool mine = (slot < slots) && (e - b <= M.short_max);
         if (!mine) e = b;
         V acc = V(0);
         int q = b + sub;
