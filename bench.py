@@ -13,7 +13,8 @@ Also reported on the same line: the FP32 product (mixed precision), the
 end-to-end product through the C ABI with host buffers, the CPU baseline
 (the reference's CSRMV_T / scale / CSRMV_N loops restated in oracle/, one
 core), the IPM time to a 1e-8 relative gap on the 2,000 x 6,000 LP (GPU,
-plain FP64 PCG), the learned part's ablation on held-out multicommodity-flow
+plain FP64 PCG, and the mixed form against it with the FP64 residual of
+every Newton solve), the learned part's ablation on held-out multicommodity-flow
 LPs, PCG iterations per second (configs 0 and 1 by default), the same
 product on the 104M-nonzero block-angular LP, the live
 roofline of the dominant kernel and the SM clocks sampled during the timed
@@ -156,22 +157,56 @@ def cpu_adat_baseline(lp, d, seconds: float = 10.0) -> dict:
             "seconds": el}
 
 
-def ipm_time(config: int = 0) -> dict:
-    """HSD IPM (the reference's HSD_Main restated) to a 1e-8 gap on the GPU backend."""
-    from help_gb300 import backend, hsd, lp as L
+def ipm_run(config: int, precision: str) -> dict:
+    """HSD IPM (the reference's HSD_Main restated) to a 1e-8 gap on the GPU
+    backend, with the FP64 residual ||rhs - G x_2|| / ||rhs|| of every Newton
+    solve read back after the solve."""
+    import ctypes as C
+
+    from help_gb300 import backend, hsd, native, lp as L
 
     lp = L.make_lp(config, 0)
-    with backend.GpuNormalEquations(pivots=L.config_pivots(config), cg_tol=1e-10, cg_max_iter=1_000_000) as g:
+    solves = []
+    with backend.GpuNormalEquations(pivots=L.config_pivots(config), precision=precision, cg_tol=1e-10,
+                                    ir_tol=1e-10, cg_max_iter=1_000_000) as g:
+        lib, ctx = g.lib, g.ctx
+
+        def solve(_c, d, b1, b2, x1, x2):
+            rc = lib.help_pcg_solve(ctx, d, b1, b2, x1, x2)
+            st = g.stats()
+            solves.append((st["rel_residual"], st["fell_back"], st["cg_iterations"], st["cg_iterations_fp32"]))
+            return rc
+
+        fns = (native.CONSTRUCT_FN(lambda _c, m, n, cp, ri, v: lib.help_pcg_construct(ctx, m, n, cp, ri, v)),
+               native.RENEW_FN(lambda _c, d: lib.help_pcg_renew(ctx, d)), native.SOLVE_FN(solve),
+               native.DESTRUCT_FN(lambda _c: lib.help_pcg_destruct(ctx)))
+        f = lambda fn: C.cast(fn, C.c_void_p).value
+        be = native.NeBackend(ctx=None, construct=f(fns[0]), renew=f(fns[1]), solve=f(fns[2]), destruct=f(fns[3]))
         t0 = time.perf_counter()
-        r = hsd.solve_lp(lp, g.ne_backend())
+        r = hsd.solve_lp(lp, be)
         wall = time.perf_counter() - t0
         st = g.stats()
+    res = np.array([s_[0] for s_ in solves]) if solves else np.zeros(1)
     return {"config": "config %d: m=%d n=%d nnz=%d" % (config, lp.m, lp.n, lp.nnz),
-            "form": "plain FP64 PCG, k=%d, cg_tol 1e-10, CG path %s" % (
-                L.config_pivots(config), {1: "graph", 2: "single cluster"}.get(int(st["cg_path_used"]), "?")),
+            "form": "%s PCG, k=%d, tol 1e-10, CG path %s" % (
+                "plain FP64" if precision == "fp64" else "FP32 CG in FP64 refinement", L.config_pivots(config),
+                {1: "graph", 2: "single cluster"}.get(int(st["cg_path_used"]), "?")),
             "seconds": round(wall, 3), "status": r["status"], "iterations": r["iterations"],
-            "rel_gap": r["rel_gap"], "primal_obj": r["primal_obj"], "cg_iterations": int(st["cg_iterations_total"]),
+            "rel_gap": r["rel_gap"], "primal_obj": r["primal_obj"], "primal_infeas": r["primal_infeas"],
+            "dual_infeas": r["dual_infeas"], "cg_iterations": int(st["cg_iterations_total"]),
+            "cg_iterations_fp32": int(sum(s_[3] for s_ in solves)), "solves": len(solves),
+            "solves_finished_in_fp64": int(sum(s_[1] for s_ in solves)),
+            "newton_residual_max": float(res.max()), "newton_residual_median": float(np.median(res)),
             "backend_seconds": round(r["backend_s"], 3)}
+
+
+def ipm_time(config: int = 0) -> dict:
+    """Plain FP64 IPM time, and the mixed form measured against it."""
+    plain = ipm_run(config, "fp64")
+    mixed = ipm_run(config, "mixed")
+    mixed["obj_rel_diff_vs_fp64"] = abs(mixed["primal_obj"] - plain["primal_obj"]) / abs(plain["primal_obj"])
+    plain["mixed"] = mixed
+    return plain
 
 
 def spmv_large(steps: int, warmup: int, local: int) -> dict:
