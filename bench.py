@@ -254,9 +254,10 @@ def spmv_large(steps: int, warmup: int, local: int) -> dict:
 
 
 def pcg_rate(config: int, iters: int, local: int) -> dict:
-    """PCG iterations per second (FP64) on the given configuration with its
-    pivot count, d log-uniform in [1e-8, 1e8]: one CG run of exactly `iters`
-    iterations (unreachable tolerance), timed on the device with CUDA events."""
+    """PCG iterations per second on the given configuration with its pivot
+    count, d log-uniform in [1e-8, 1e8]: one CG run of exactly `iters`
+    iterations (unreachable tolerance) in FP64 and one in FP32 (the mixed
+    form's inner solver), timed on the device with CUDA events."""
     from help_gb300 import backend, lp as L
 
     lp = L.make_lp(config, 0)
@@ -264,18 +265,22 @@ def pcg_rate(config: int, iters: int, local: int) -> dict:
     d = np.exp(rng.uniform(np.log(1e-8), np.log(1e8), lp.n))
     b = rng.standard_normal(lp.m)
     k = L.config_pivots(config)
-    with backend.GpuNormalEquations(pivots=k, cg_tol=1e-300, cg_max_iter=iters, device=local) as g:
+    out = {}
+    with backend.GpuNormalEquations(pivots=k, precision="mixed", cg_tol=1e-300, cg_max_iter=iters,
+                                    device=local) as g:
         g.LinearEquation_Construct(lp)
         g.RenewLinearEquation(d)
         renew_ms = g.stats()["renew_ms"]
-        g.cg(b)  # graph capture and warm-up
-        _, it = g.cg(b)
-        st = g.stats()
-    us = st["cg_kernel_ms"] * 1e3 / max(it, 1)
-    return {"workload": "config %d: m=%d n=%d nnz=%d, k=%d, nnz(C)=%d" % (config, lp.m, lp.n, lp.nnz, k, st["nnz_c"]),
-            "iterations": int(it), "us_per_iteration": round(us, 2), "iterations_per_s": round(1e6 / us, 1),
-            "renew_ms": round(renew_ms, 2),
-            "path": {1: "graph", 2: "single cluster"}.get(int(st["cg_path_used"]), "?")}
+        for prec in ("f64", "f32"):
+            g.cg(b, fp32=prec == "f32")  # graph capture and warm-up
+            _, it = g.cg(b, fp32=prec == "f32")
+            st = g.stats()
+            us = st["cg_kernel_ms"] * 1e3 / max(it, 1)
+            out[prec] = {"iterations": int(it), "us_per_iteration": round(us, 2), "iterations_per_s": round(1e6 / us, 1)}
+    out.update({"workload": "config %d: m=%d n=%d nnz=%d, k=%d, nnz(C)=%d" % (config, lp.m, lp.n, lp.nnz, k, st["nnz_c"]),
+                "renew_ms": round(renew_ms, 2),
+                "path": {1: "graph", 2: "single cluster"}.get(int(st["cg_path_used"]), "?")})
+    return out
 
 
 def learned_ablation() -> dict:

@@ -164,11 +164,12 @@ class GpuNormalEquations:
         self._check(self.lib.help_pcg_get_pivots(self.ctx, native.ptr(piv), native.ptr(dg), native.ptr(ds)))
         return piv[:k], dg, ds
 
-    def cg(self, b):
+    def cg(self, b, fp32: bool = False):
         b = _f64(b, self.m)
         x = np.empty(self.m)
         it = C.c_int64()
-        self._check(self.lib.help_pcg_cg(self.ctx, native.ptr(b), native.ptr(x), C.byref(it)))
+        fn = self.lib.help_pcg_cg_f32 if fp32 else self.lib.help_pcg_cg
+        self._check(fn(self.ctx, native.ptr(b), native.ptr(x), C.byref(it)))
         return x, int(it.value)
 
     def adat(self, w):

@@ -1051,6 +1051,33 @@ int help_pcg_cg(help_pcg* ctx, const double* b, double* x, int64_t* iters) {
     return d2h(ctx, x, ctx->x.as<double>(), ctx->m);
 }
 
+int help_pcg_cg_f32(help_pcg* ctx, const double* b, double* x, int64_t* iters) {
+    if (!ctx || !b || !x) return HELP_E_ARG;
+    if (!ctx->renewed) return fail(ctx, HELP_E_ARG, "cg_f32: renew first");
+    if (ctx->opt.precision != HELP_PREC_MIXED)
+        return fail(ctx, HELP_E_ARG, "cg_f32: the context holds no FP32 copies (create it with HELP_PREC_MIXED)");
+    CK(cudaSetDevice(ctx->device));
+    const int m = ctx->m;
+    int rc = h2d(ctx, ctx->r0.as<double>(), b, m);
+    if (rc) return rc;
+    CK(vec_to_f32(ctx->r0.as<double>(), ctx->r032.as<float>(), m, ctx->stream));
+    CK(vec_fill_f32(ctx->x32.as<float>(), 0.0f, m, ctx->stream));
+    CgResult res;
+    ctx->solve_kernel_ms = 0;
+    ctx->solve_launches = 0;
+    ctx->solve_iters_f32 = 0;
+    rc = run_pcg<float>(ctx, ctx->x32.as<float>(), ctx->r032.as<float>(), ctx->opt.cg_tol, ctx->opt.cg_max_iter, 0, &res);
+    if (rc) return rc;
+    if (iters) *iters = res.iterations;
+    ctx->stats.cg_iterations = res.iterations;
+    ctx->stats.cg_iterations_fp32 = res.iterations;
+    ctx->stats.cg_kernel_ms = ctx->solve_kernel_ms;
+    ctx->stats.cg_launches = ctx->solve_launches;
+    CK(vec_fill(ctx->x.as<double>(), 0.0, m, ctx->stream));
+    CK(vec_add_f32(ctx->x.as<double>(), ctx->x32.as<float>(), m, ctx->stream));
+    return d2h(ctx, x, ctx->x.as<double>(), m);
+}
+
 int help_pcg_attach_mlp(help_pcg* ctx, help_mlp* mlp) {
     if (!ctx) return HELP_E_ARG;
     if (mlp && help_mlp_device(mlp) != ctx->device)

@@ -176,7 +176,7 @@ GPU_SYMBOLS = [
     "help_pcg_default_options", "help_pcg_create", "help_pcg_free", "help_pcg_construct",
     "help_pcg_renew", "help_pcg_solve", "help_pcg_destruct", "help_pcg_get_stats",
     "help_pcg_last_error", "help_pcg_matvec", "help_pcg_matvec_dev", "help_pcg_precond_apply",
-    "help_pcg_get_pivots", "help_pcg_cg", "help_adat_assemble", "help_adat_matvec_noalloc",
+    "help_pcg_get_pivots", "help_pcg_cg", "help_pcg_cg_f32", "help_adat_assemble", "help_adat_matvec_noalloc",
     "help_mlp_create", "help_mlp_free", "help_mlp_last_error", "help_mlp_set_params", "help_mlp_get_params",
     "help_mlp_forward", "help_mlp_loss_grad", "help_mlp_train_step", "help_pcg_attach_mlp", "help_pcg_features",
 ]
@@ -220,6 +220,7 @@ def gpu_lib() -> C.CDLL:
         lib.help_pcg_precond_apply.argtypes = [vp, dp, dp]
         lib.help_pcg_get_pivots.argtypes = [vp, dp, dp, dp]
         lib.help_pcg_cg.argtypes = [vp, dp, dp, C.POINTER(C.c_int64)]
+        lib.help_pcg_cg_f32.argtypes = [vp, dp, dp, C.POINTER(C.c_int64)]
         lib.help_adat_assemble.argtypes = [vp, dp, dp, dp, dp, C.POINTER(C.c_int64)]
         lib.help_adat_matvec_noalloc.argtypes = [i32, i32, i64] + [vp] * 10
         lib.help_mlp_create.argtypes = [i32, C.POINTER(C.c_void_p)]

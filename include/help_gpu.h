@@ -148,6 +148,10 @@ int help_pcg_get_pivots(help_pcg* ctx, int32_t* pivots, double* diag_g, double* 
  * preconditioner (ConjugateGradient, PCG.cpp:296-395); returns iterations in
  * *iters; stats cg_iterations / cg_kernel_ms / cg_launches describe this run. */
 int help_pcg_cg(help_pcg* ctx, const double* b, double* x, int64_t* iters);
+/* The same run in FP32 (vectors and matrices in FP32, dot products and the
+ * pivot block in FP64) on a context created with HELP_PREC_MIXED: the inner
+ * solver of the mixed form, alone. */
+int help_pcg_cg_f32(help_pcg* ctx, const double* b, double* x, int64_t* iters);
 
 /* Explicit A diag(w) A^T, upper triangle incl. diagonal, CSR with columns
  * sorted in each row (ADAt_Allocate + ADAt_Calc, Helper.cpp:215-377; the

@@ -218,3 +218,20 @@ def test_long_rows_repeatable_and_fp32():
             outs.append(y32.cpu().numpy().astype(np.float64))
         assert np.array_equal(outs[0], outs[1])
         assert rel(outs[0], y1) < 1e-5
+
+
+@pytest.mark.parametrize("name", ["random", "mcf"])
+def test_cg_f32_agrees_with_fp64(name):
+    """The mixed form's FP32 inner CG alone (help_pcg_cg_f32) reaches the FP64
+    solution to FP32 accuracy: 1e-3 relative at a 1e-5 residual reduction."""
+    lp = CASES[name]()
+    rng = np.random.default_rng(13)
+    d = np.exp(rng.uniform(-3, 3, lp.n))
+    b = rng.standard_normal(lp.m)
+    with backend.GpuNormalEquations(pivots=16, precision="mixed", cg_tol=1e-5, cg_max_iter=20000) as g:
+        g.LinearEquation_Construct(lp)
+        g.RenewLinearEquation(d)
+        x64, it64 = g.cg(b)
+        x32, it32 = g.cg(b, fp32=True)
+    assert it32 < 20000
+    assert rel(x32, x64) < 1e-3
