@@ -13,8 +13,9 @@ Also reported on the same line: the FP32 product (mixed precision), the
 end-to-end product through the C ABI with host buffers, the CPU baseline
 (the reference's CSRMV_T / scale / CSRMV_N loops restated in oracle/, one
 core), the IPM time to a 1e-8 relative gap on the 2,000 x 6,000 LP (GPU,
-plain FP64 PCG, and the mixed form against it with the FP64 residual of
-every Newton solve), the learned part's ablation on held-out multicommodity-flow
+plain FP64 PCG, the mixed form against it with the FP64 residual of every
+Newton solve, and the direct form with every row a pivot), the learned
+part's ablation on held-out multicommodity-flow
 LPs, PCG iterations per second (configs 0 and 1 by default), the same
 product on the 104M-nonzero block-angular LP, the live
 roofline of the dominant kernel and the SM clocks sampled during the timed
@@ -157,7 +158,7 @@ def cpu_adat_baseline(lp, d, seconds: float = 10.0) -> dict:
             "seconds": el}
 
 
-def ipm_run(config: int, precision: str) -> dict:
+def ipm_run(config: int, precision: str, pivots: int | None = None) -> dict:
     """HSD IPM (the reference's HSD_Main restated) to a 1e-8 gap on the GPU
     backend, with the FP64 residual ||rhs - G x_2|| / ||rhs|| of every Newton
     solve read back after the solve."""
@@ -166,8 +167,9 @@ def ipm_run(config: int, precision: str) -> dict:
     from help_gb300 import backend, hsd, native, lp as L
 
     lp = L.make_lp(config, 0)
+    k = L.config_pivots(config) if pivots is None else min(pivots, lp.m)
     solves = []
-    with backend.GpuNormalEquations(pivots=L.config_pivots(config), precision=precision, cg_tol=1e-10,
+    with backend.GpuNormalEquations(pivots=k, precision=precision, cg_tol=1e-10,
                                     ir_tol=1e-10, cg_max_iter=1_000_000) as g:
         lib, ctx = g.lib, g.ctx
 
@@ -189,7 +191,7 @@ def ipm_run(config: int, precision: str) -> dict:
     res = np.array([s_[0] for s_ in solves]) if solves else np.zeros(1)
     return {"config": "config %d: m=%d n=%d nnz=%d" % (config, lp.m, lp.n, lp.nnz),
             "form": "%s PCG, k=%d, tol 1e-10, CG path %s" % (
-                "plain FP64" if precision == "fp64" else "FP32 CG in FP64 refinement", L.config_pivots(config),
+                "plain FP64" if precision == "fp64" else "FP32 CG in FP64 refinement", k,
                 {1: "graph", 2: "single cluster"}.get(int(st["cg_path_used"]), "?")),
             "seconds": round(wall, 3), "status": r["status"], "iterations": r["iterations"],
             "rel_gap": r["rel_gap"], "primal_obj": r["primal_obj"], "primal_infeas": r["primal_infeas"],
@@ -206,6 +208,10 @@ def ipm_time(config: int = 0) -> dict:
     mixed = ipm_run(config, "mixed")
     mixed["obj_rel_diff_vs_fp64"] = abs(mixed["primal_obj"] - plain["primal_obj"]) / abs(plain["primal_obj"])
     plain["mixed"] = mixed
+    # direct form: every row a pivot, i.e. the full Cholesky of A D^-1 A^T
+    direct = ipm_run(config, "fp64", pivots=1 << 30)
+    direct["obj_rel_diff_vs_fp64"] = abs(direct["primal_obj"] - plain["primal_obj"]) / abs(plain["primal_obj"])
+    plain["direct"] = direct
     return plain
 
 

@@ -235,3 +235,27 @@ def test_cg_f32_agrees_with_fp64(name):
         x32, it32 = g.cg(b, fp32=True)
     assert it32 < 20000
     assert rel(x32, x64) < 1e-3
+
+
+@pytest.mark.parametrize("name", ["random", "block"])
+def test_direct_form_all_rows_pivots(name):
+    """pivots = m: the partial Cholesky becomes the full factorisation of
+    A D^-1 A^T, CG converges in one or two iterations, and the solve agrees
+    with the oracle's (a direct solve; the second oracle for the PCG path)."""
+    lp = CASES[name]()
+    rng = np.random.default_rng(14)
+    d = np.exp(rng.uniform(-4, 4, lp.n))
+    b1 = rng.standard_normal(lp.n)
+    b2 = rng.standard_normal(lp.m)
+    with backend.GpuNormalEquations(pivots=lp.m, cg_tol=1e-12, cg_max_iter=100) as g:
+        g.LinearEquation_Construct(lp)
+        g.RenewLinearEquation(d)
+        x1, x2 = g.SolveLinearEquation(d, b1, b2)
+        st = g.stats()
+    assert st["pivots"] == lp.m and st["nnz_c"] == 0
+    assert st["cg_iterations"] <= 3
+    ora = ob.OracleNormalEquations(pivots=10, rule=ob.PIVOT_GREEDY, tol=1e-14, max_iter=200000)
+    ora.LinearEquation_Construct(lp)
+    ox1, ox2 = ora.SolveLinearEquation(d, b1, b2)
+    assert rel(x2, ox2) < 1e-8
+    assert rel(x1, ox1) < 1e-8
