@@ -27,37 +27,41 @@ __global__ void k_potrf_diag(double* __restrict__ A, int k, int j0, int kb, doub
                              const double* __restrict__ orig_diag, int* __restrict__ regularised) {
     __shared__ double L[NB][NB + 1];
     __shared__ double X[NB][NB + 1];
+    __shared__ double fl[NB], rdiag[NB];
     const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
     L[ty][tx] = (ty < kb && tx < kb && tx <= ty) ? A[(size_t)(j0 + ty) * k + j0 + tx] : 0.0;
     X[ty][tx] = 0.0;
+    if (ty == 0) fl[tx] = tx < kb ? fmax(1.0e-14 * orig_diag[j0 + tx], 1.0e-300) : 1.0;
     __syncthreads();
     for (int c = 0; c < kb; ++c) {
         if (threadIdx.x == 0) {
             double piv = L[c][c];
-            const double fl = fmax(1.0e-14 * orig_diag[j0 + c], 1.0e-300);
-            if (!(piv > fl)) {
-                piv = fl;
+            if (!(piv > fl[c])) {
+                piv = fl[c];
                 atomicAdd(regularised, 1);
             }
-            L[c][c] = sqrt(piv);
+            const double sq = sqrt(piv);
+            L[c][c] = sq;
+            rdiag[c] = 1.0 / sq;
         }
         __syncthreads();
-        if (tx == 0 && ty > c && ty < kb) L[ty][c] /= L[c][c];
+        if (tx == 0 && ty > c && ty < kb) L[ty][c] *= rdiag[c];
         __syncthreads();
         if (ty > c && ty < kb && tx > c && tx <= ty) L[ty][tx] = fma(-L[ty][c], L[tx][c], L[ty][tx]);
         __syncthreads();
     }
-    // inverse of the lower-triangular block: thread tx < kb owns column tx
-    if (ty == 0 && tx < kb) {
-        const int c = tx;
-        X[c][c] = 1.0 / L[c][c];
-        for (int r = c + 1; r < kb; ++r) {
-            double s = 0.0;
-            for (int l = c; l < r; ++l) s = fma(L[r][l], X[l][c], s);
-            X[r][c] = -s / L[r][r];
-        }
-    }
+    // inverse of the lower-triangular block by rows: X[r][c] for every column
+    // c < r at once (thread tx = c), using the rows above it
+    if (ty == 0 && tx < kb) X[tx][tx] = rdiag[tx];
     __syncthreads();
+    for (int r = 1; r < kb; ++r) {
+        if (ty == 0 && tx < r) {
+            double s = 0.0;
+            for (int l = tx; l < r; ++l) s = fma(L[r][l], X[l][tx], s);
+            X[r][tx] = -s * rdiag[r];
+        }
+        __syncthreads();
+    }
     if (ty < kb && tx < kb && tx <= ty) A[(size_t)(j0 + ty) * k + j0 + tx] = L[ty][tx];
     linv[ty * NB + tx] = (ty < kb && tx < kb) ? X[ty][tx] : 0.0;
 }
@@ -119,46 +123,99 @@ __global__ void k_syrk_lower(double* __restrict__ A, int k, int j0, int kb, int 
         }
 }
 
-// One step of the blocked triangular inverse: for every block column j with
-// i = j + s < nblk, X_ij = -Linv_ii * sum_{l=j}^{i-1} L_il X_lj.
-__global__ void k_trtri_step(const double* __restrict__ L, double* __restrict__ X, int k, int nblk, int s,
-                             const double* __restrict__ linv_all) {
-    const int j = blockIdx.x, i = j + s;
-    if (i >= nblk) return;
-    __shared__ double Lt[NB][NB + 1];
-    __shared__ double Xt[NB][NB + 1];
-    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
-    double acc = 0.0;
-    for (int l = j; l < i; ++l) {
-        const int rL = i * NB + ty, cL = l * NB + tx;
-        Lt[ty][tx] = (rL < k && cL < k) ? L[(size_t)rL * k + cL] : 0.0;
-        const int rX = l * NB + ty, cX = j * NB + tx;
-        Xt[ty][tx] = (rX < k && cX < k) ? X[(size_t)rX * k + cX] : 0.0;
+// Triangular inverse X = L^-1 by recursive halving, level by level: with
+// L = [L_A 0; B L_C] on a node of 2 n rows, X = [X_A 0; -X_C B X_A X_C].
+// Level n = 32, 64, ... doubles the nodes' size; each level is two batched
+// GEMM launches over all its nodes (T = B X_A, then X_21 = -X_C T), so the
+// inverse takes 2 log2(nblk) launches instead of nblk dependent steps.  X
+// has the padded order kp = 32 * 2^ceil(log2 nblk); rows and columns past k
+// are an identity block that couples to nothing.  The zeros above the
+// diagonal of X_A and X_C are skipped a K-slab at a time.
+constexpr int TG = 64;   // output tile
+constexpr int TK = 16;   // K slab
+
+// mode 0: T = B X_A   (A operand = L rows o+n.., cols o..; B operand = X_A)
+// mode 1: X21 = -X_C T (A operand = X_C; B operand = T)
+template <int MODE>
+__global__ void __launch_bounds__(256) k_trtri_level(const double* __restrict__ L, int k, double* __restrict__ X,
+                                                     int kp, double* __restrict__ T, int n) {
+    const int node = blockIdx.z;
+    const int o = node * 2 * n;
+    if (o + n >= k) return;  // B is entirely past k: this node's X_21 stays zero
+    const int i0 = blockIdx.y * TG, j0 = blockIdx.x * TG;
+    if (i0 >= n || j0 >= n) return;
+    double* Tn = T + (size_t)node * n * n;
+    __shared__ double As[TG][TK + 1];
+    __shared__ double Bs[TK][TG + 1];
+    const int tr = threadIdx.x / 16, tc = threadIdx.x % 16;
+    double acc[4][4];
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
+#pragma unroll
+        for (int b = 0; b < 4; ++b) acc[a][b] = 0.0;
+    // K range: mode 0 skips l < j0 (X_A lower), mode 1 skips l > i0 + TG - 1 (X_C lower)
+    const int kbeg = MODE == 0 ? (j0 / TK) * TK : 0;
+    const int kend = MODE == 0 ? n : min(n, i0 + TG);
+    for (int l0 = kbeg; l0 < kend; l0 += TK) {
+        for (int t = threadIdx.x; t < TG * TK; t += blockDim.x) {
+            const int r = t / TK, c = t % TK;
+            const int gi = i0 + r, gl = l0 + c;
+            double v = 0.0;
+            if (gi < n && gl < n) {
+                if (MODE == 0) {
+                    const int row = o + n + gi, col = o + gl;
+                    v = (row < k && col < k) ? L[(size_t)row * k + col] : 0.0;
+                } else {
+                    v = X[(size_t)(o + n + gi) * kp + (o + n + gl)];
+                }
+            }
+            As[r][c] = v;
+        }
+        for (int t = threadIdx.x; t < TK * TG; t += blockDim.x) {
+            const int r = t / TG, c = t % TG;
+            const int gl = l0 + r, gj = j0 + c;
+            double v = 0.0;
+            if (gl < n && gj < n) v = MODE == 0 ? X[(size_t)(o + gl) * kp + (o + gj)] : Tn[(size_t)gl * n + gj];
+            Bs[r][c] = v;
+        }
         __syncthreads();
-#pragma unroll 8
-        for (int c = 0; c < NB; ++c) acc = fma(Lt[ty][c], Xt[c][tx], acc);
+#pragma unroll
+        for (int c = 0; c < TK; ++c) {
+            double va[4], vb[4];
+#pragma unroll
+            for (int a = 0; a < 4; ++a) va[a] = As[tr + 16 * a][c];
+#pragma unroll
+            for (int b = 0; b < 4; ++b) vb[b] = Bs[c][tc + 16 * b];
+#pragma unroll
+            for (int a = 0; a < 4; ++a)
+#pragma unroll
+                for (int b = 0; b < 4; ++b) acc[a][b] = fma(va[a], vb[b], acc[a][b]);
+        }
         __syncthreads();
     }
-    Xt[ty][tx] = acc;
-    Lt[ty][tx] = linv_all[(size_t)i * NB * NB + ty * NB + tx];
-    __syncthreads();
-    double out = 0.0;
-#pragma unroll 8
-    for (int c = 0; c < NB; ++c) out = fma(Lt[ty][c], Xt[c][tx], out);
-    const int r = i * NB + ty, cc = j * NB + tx;
-    if (r < k && cc < k) X[(size_t)r * k + cc] = -out;
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
+#pragma unroll
+        for (int b = 0; b < 4; ++b) {
+            const int gi = i0 + tr + 16 * a, gj = j0 + tc + 16 * b;
+            if (gi < n && gj < n) {
+                if (MODE == 0) Tn[(size_t)gi * n + gj] = acc[a][b];
+                else X[(size_t)(o + n + gi) * kp + (o + gj)] = -acc[a][b];
+            }
+        }
 }
 
-__global__ void k_place_linv(double* __restrict__ X, int k, int nblk, const double* __restrict__ linv_all) {
+// Diagonal blocks of X: the 32 x 32 inverses, identity past k.
+__global__ void k_place_linv(double* __restrict__ X, int kp, int nblk, const double* __restrict__ linv_all) {
     const int b = blockIdx.x;
     const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
-    const int r = b * NB + ty, c = b * NB + tx;
-    if (r < k && c < k) X[(size_t)r * k + c] = linv_all[(size_t)b * NB * NB + ty * NB + tx];
+    const double v = b < nblk ? linv_all[(size_t)b * NB * NB + ty * NB + tx] : (tx == ty ? 1.0 : 0.0);
+    X[(size_t)(b * NB + ty) * kp + b * NB + tx] = v;
 }
 
 // W = X^T X for lower-triangular X: W[a][b] = sum_{l >= max(a,b)} X[l][a] X[l][b],
 // lower tiles computed, both triangles written.
-__global__ void k_xtx(const double* __restrict__ X, double* __restrict__ W, int k) {
+__global__ void k_xtx(const double* __restrict__ X, int ldx, double* __restrict__ W, int k) {
     const int ta = blockIdx.y, tb = blockIdx.x;
     if (tb > ta) return;
     __shared__ double Xa[16][64 + 1];
@@ -174,8 +231,8 @@ __global__ void k_xtx(const double* __restrict__ X, double* __restrict__ W, int 
         for (int t = threadIdx.x; t < 16 * 64; t += blockDim.x) {
             const int r = t / 64, c = t % 64;
             const int l = l0 + r;
-            Xa[r][c] = (l < k && a0 + c < k) ? X[(size_t)l * k + a0 + c] : 0.0;
-            Xb[r][c] = (l < k && b0 + c < k) ? X[(size_t)l * k + b0 + c] : 0.0;
+            Xa[r][c] = (l < k && a0 + c < k) ? X[(size_t)l * ldx + a0 + c] : 0.0;
+            Xb[r][c] = (l < k && b0 + c < k) ? X[(size_t)l * ldx + b0 + c] : 0.0;
         }
         __syncthreads();
 #pragma unroll
@@ -210,17 +267,28 @@ __global__ void k_copy_diag(const double* __restrict__ A, int k, double* __restr
 
 }  // namespace
 
+// padded order of X: 32 * (smallest power of two >= the block count)
+int padded_order(int k) {
+    const int nblk = (k + NB - 1) / NB;
+    int p = 1;
+    while (p < nblk) p *= 2;
+    return p * NB;
+}
+
 size_t dense_work_elems(int k) {
     const size_t nblk = (size_t)(k + NB - 1) / NB;
-    return (size_t)k * k + nblk * NB * NB + (size_t)k + 64;
+    const size_t kp = (size_t)padded_order(k);
+    return kp * kp + kp * kp / 4 + nblk * NB * NB + (size_t)k + 64;
 }
 
 cudaError_t dense_spd_inverse(double* g11, double* W, double* work, int k, int* regularised, cudaStream_t st) {
     if (k <= 0) return cudaSuccess;
     const int nblk = (k + NB - 1) / NB;
-    double* X = work;                                   // k*k
-    double* linv_all = work + (size_t)k * k;            // nblk * NB * NB
-    double* orig_diag = linv_all + (size_t)nblk * NB * NB;  // k
+    const int kp = padded_order(k);
+    double* X = work;                                        // kp * kp
+    double* T = X + (size_t)kp * kp;                          // kp * kp / 4 (level temporaries)
+    double* linv_all = T + (size_t)kp * kp / 4;               // nblk * NB * NB
+    double* orig_diag = linv_all + (size_t)nblk * NB * NB;    // k
     k_copy_diag<<<(k + 255) / 256, 256, 0, st>>>(g11, k, orig_diag);
     for (int jb = 0; jb < nblk; ++jb) {
         const int j0 = jb * NB, kb = (k - j0 < NB) ? k - j0 : NB;
@@ -232,12 +300,17 @@ cudaError_t dense_spd_inverse(double* g11, double* W, double* work, int k, int* 
             k_syrk_lower<<<dim3(tiles, tiles), 256, 0, st>>>(g11, k, j0, kb, j0 + kb);
         }
     }
-    cudaError_t e = cudaMemsetAsync(X, 0, sizeof(double) * (size_t)k * k, st);
+    cudaError_t e = cudaMemsetAsync(X, 0, sizeof(double) * (size_t)kp * kp, st);
     if (e != cudaSuccess) return e;
-    k_place_linv<<<nblk, NB * NB, 0, st>>>(X, k, nblk, linv_all);
-    for (int s = 1; s < nblk; ++s) k_trtri_step<<<nblk - s, NB * NB, 0, st>>>(g11, X, k, nblk, s, linv_all);
+    k_place_linv<<<kp / NB, NB * NB, 0, st>>>(X, kp, nblk, linv_all);
+    for (int n = NB; n < kp; n *= 2) {
+        const int tiles = (n + TG - 1) / TG, nodes = kp / (2 * n);
+        const dim3 grid(tiles, tiles, nodes);
+        k_trtri_level<0><<<grid, 256, 0, st>>>(g11, k, X, kp, T, n);
+        k_trtri_level<1><<<grid, 256, 0, st>>>(g11, k, X, kp, T, n);
+    }
     const int tiles = (k + 63) / 64;
-    k_xtx<<<dim3(tiles, tiles), 256, 0, st>>>(X, W, k);
+    k_xtx<<<dim3(tiles, tiles), 256, 0, st>>>(X, kp, W, k);
     return cudaGetLastError();
 }
 
