@@ -55,9 +55,10 @@ struct RowPlan {
 // at most kPerLane* nonzeros of an average row.  Measured on GB300 (config 1,
 // 2 and 4 passes): FP32 is fastest at ~4 per lane down to groups of 2 (the
 // FP32 pass over 6-nonzero rows 74 -> 45 us against a floor of 8 lanes);
-// FP64 at ~8 per lane (its shuffle adds go through the slow FP64 pipe).
+// FP64 at 7 per lane: rows of 13 want 2 lanes (4 lanes cost 40 %), rows of
+// 21 want 4 (8 lanes cost 13 %), rows of 32 want 8 (28.7 -> 26.6 us).
 constexpr int kGminF64 = 2;
-constexpr int kPerLaneF64 = 8;
+constexpr int kPerLaneF64 = 7;
 constexpr int kGminF32 = 2;
 constexpr int kPerLaneF32 = 4;
 

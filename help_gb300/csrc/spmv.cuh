@@ -7,7 +7,7 @@
 // Rows are split by length when the matrix is planned (host, once per matrix
 // and precision; see items.cpp):
 //   * short rows (len <= short_max = 32 G): a group of G lanes per row, G a
-//     power of two (at least 2) chosen so each lane handles ~8 (FP64) or ~4
+//     power of two (at least 2) chosen so each lane handles <= 7 (FP64) or 4
 //     (FP32) nonzeros of an average row.  A warp covers 32 / G rows -- in
 //     index order, so its loads sweep one contiguous span of the value and
 //     index arrays, or, for matrices whose row lengths vary a lot, by
