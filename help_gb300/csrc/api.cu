@@ -119,31 +119,16 @@ SpmvView<V> view(const RowPlan& P, const DevMem& ptr, const DevMem& idx, const D
 int spmv_blocks(help_pcg* ctx) { return ctx->num_sms * 8; }
 constexpr int kSpmvThreads = 256;
 
-int ensure_stage(help_pcg* ctx, size_t elems) {
-    if (ctx->h_stage_elems >= elems) return HELP_OK;
-    if (ctx->h_stage) cudaFreeHost(ctx->h_stage);
-    ctx->h_stage = nullptr;
-    ctx->h_stage_elems = 0;
-    CK(cudaMallocHost((void**)&ctx->h_stage, sizeof(double) * elems));
-    ctx->h_stage_elems = elems;
-    return HELP_OK;
-}
-
-// host -> device through the pinned staging buffer
+// Host arrays of the caller straight to / from the copy engine.  A copy from
+// pageable memory returns once the source has been taken (the caller may
+// reuse it); the copy back is waited for, pinned or not.
 int h2d(help_pcg* ctx, double* dst, const double* src, size_t n) {
-    int rc = ensure_stage(ctx, n);
-    if (rc) return rc;
-    std::memcpy(ctx->h_stage, src, sizeof(double) * n);
-    CK(cudaMemcpyAsync(dst, ctx->h_stage, sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream));
-    CK(cudaStreamSynchronize(ctx->stream));
+    CK(cudaMemcpyAsync(dst, src, sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream));
     return HELP_OK;
 }
 int d2h(help_pcg* ctx, double* dst, const double* src, size_t n) {
-    int rc = ensure_stage(ctx, n);
-    if (rc) return rc;
-    CK(cudaMemcpyAsync(ctx->h_stage, src, sizeof(double) * n, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaMemcpyAsync(dst, src, sizeof(double) * n, cudaMemcpyDeviceToHost, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
-    std::memcpy(dst, ctx->h_stage, sizeof(double) * n);
     return HELP_OK;
 }
 
@@ -724,7 +709,6 @@ void help_pcg_free(help_pcg* ctx) {
     help_pcg_destruct(ctx);
     ctx->ctrl.release();
     ctx->partials.release();
-    if (ctx->h_stage) cudaFreeHost(ctx->h_stage);
     for (int s = 0; s < 2; ++s)
         if (ctx->graph_exec[s]) cudaGraphExecDestroy(ctx->graph_exec[s]);
     if (ctx->h_sc) cudaFreeHost(ctx->h_sc);

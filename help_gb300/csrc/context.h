@@ -112,9 +112,6 @@ struct help_pcg {
     help::DevMem ctrl;
     help::DevMem adat_tmp;
 
-    // host staging (pinned)
-    double* h_stage = nullptr;
-    size_t h_stage_elems = 0;
 
     const double* last_d = nullptr;
     bool have_prev_x2 = false;
