@@ -454,16 +454,30 @@ int read_int(help_pcg* ctx, const int* dev, int* out) {
     return HELP_OK;
 }
 
-// Features of the current renew into X (BF16 [m][16]) with the attached
-// model's normalisation.
-int learned_features(help_pcg* ctx, __nv_bfloat16* X, float* R) {
+// Features of the current renew for solve slot `slot` into X (BF16 [m][16],
+// the attached model's normalisation) or, X null, raw into R.  D_S is the
+// uncorrected one.
+int learned_features(help_pcg* ctx, int slot, __nv_bfloat16* X, float* R) {
     const int prev = ctx->x2_cur ^ 1;
-    const double* xprev = ctx->x2_have[prev][0] ? ctx->x2h[prev][0].as<double>() : nullptr;
+    const double* xprev = ctx->x2_have[prev][slot] ? ctx->x2h[prev][slot].as<double>() : nullptr;
     double* part = ctx->partials.as<double>() + 4096;
     if (xprev) CK(vec_sumsq(xprev, ctx->m, part, part + 2048, ctx->stream));
-    CK(mlp_features(ctx->rp.as<int>(), ctx->ci.as<int>(), ctx->d.as<double>(), ctx->diag.as<double>(),
-                    ctx->dsinv.as<double>(), ctx->pivpos.as<int>(), xprev, part + 2048, ctx->m,
-                    ctx->mlp ? help_mlp_device_weights(ctx->mlp) : nullptr, X, R, ctx->stream));
+    const double* dsinv = ctx->mlp_active ? ctx->dsinv_plain.as<double>() : ctx->dsinv.as<double>();
+    CK(mlp_features(ctx->rp.as<int>(), ctx->ci.as<int>(), ctx->d.as<double>(), ctx->diag.as<double>(), dsinv,
+                    ctx->pivpos.as<int>(), xprev, part + 2048, ctx->have_dprev ? ctx->d_prev.as<double>() : nullptr,
+                    ctx->m, ctx->mlp ? help_mlp_device_weights(ctx->mlp) : nullptr, X, R, ctx->stream));
+    return HELP_OK;
+}
+
+// Features of `slot` and the model's outputs for them into mlp_out.
+int learned_forward(help_pcg* ctx, int slot) {
+    const int m = ctx->m;
+    CK(ctx->mlp_x.ensure(2 * (size_t)HELP_MLP_IN * m));
+    CK(ctx->mlp_out.ensure(sizeof(float) * HELP_MLP_OUT * (size_t)m));
+    int rc = learned_features(ctx, slot, ctx->mlp_x.as<__nv_bfloat16>(), nullptr);
+    if (rc) return rc;
+    CK(mlp_forward(ctx->mlp_x.as<__nv_bfloat16>(), m, help_mlp_device_weights(ctx->mlp), ctx->mlp_out.as<float>(),
+                   nullptr, nullptr, ctx->num_sms, ctx->stream));
     return HELP_OK;
 }
 
@@ -471,13 +485,9 @@ int learned_features(help_pcg* ctx, __nv_bfloat16* X, float* R) {
 // (the plain one kept for the fallback).
 int learned_renew(help_pcg* ctx) {
     const int m = ctx->m;
-    CK(ctx->mlp_x.ensure(2 * (size_t)HELP_MLP_IN * m));
-    CK(ctx->mlp_out.ensure(sizeof(float) * HELP_MLP_OUT * (size_t)m));
     CK(ctx->dsinv_plain.ensure(8 * (size_t)m));
-    int rc = learned_features(ctx, ctx->mlp_x.as<__nv_bfloat16>(), nullptr);
+    int rc = learned_forward(ctx, 0);  // the correction is slot 0's output
     if (rc) return rc;
-    CK(mlp_forward(ctx->mlp_x.as<__nv_bfloat16>(), m, help_mlp_device_weights(ctx->mlp), ctx->mlp_out.as<float>(),
-                   nullptr, nullptr, ctx->num_sms, ctx->stream));
     CK(cudaMemcpyAsync(ctx->dsinv_plain.p, ctx->dsinv.p, 8 * (size_t)m, cudaMemcpyDeviceToDevice, ctx->stream));
     const bool mixed = ctx->opt.precision == HELP_PREC_MIXED;
     CK(mlp_apply_diag(ctx->mlp_out.as<float>(), ctx->pivpos.as<int>(), ctx->dsinv.as<double>(),
@@ -504,6 +514,10 @@ int learned_warm_start(help_pcg* ctx, int slot, bool* used) {
     const int prev = ctx->x2_cur ^ 1;
     if (!ctx->x2_have[prev][slot]) return HELP_OK;
     const int m = ctx->m;
+    if (slot > 0) {  // this slot's own features (slot 0's came with the renew)
+        const int rc = learned_forward(ctx, slot);
+        if (rc) return rc;
+    }
     double* x = ctx->x.as<double>();
     double* gv = ctx->res.as<double>();
     CK(mlp_warm_vector(ctx->mlp_out.as<float>(), ctx->x2h[prev][slot].as<double>(), x, m, ctx->stream));
@@ -529,6 +543,13 @@ int renew_impl(help_pcg* ctx, const double* d_host) {
     const int m = ctx->m, n = ctx->n;
     const bool mixed = ctx->opt.precision == HELP_PREC_MIXED;
     DevCtrl* c = ctrl_of(ctx);
+    // the learned part's features compare d with the previous renew's
+    ctx->have_dprev = false;
+    if (ctx->mlp && ctx->renewed) {
+        CK(ctx->d_prev.ensure(8 * (size_t)n));
+        CK(cudaMemcpyAsync(ctx->d_prev.p, ctx->d.p, 8 * (size_t)n, cudaMemcpyDeviceToDevice, ctx->stream));
+        ctx->have_dprev = true;
+    }
     int rc = h2d(ctx, ctx->d.as<double>(), d_host, n);
     if (rc) return rc;
     CK(renew_inv_sqrt(ctx->d.as<double>(), ctx->s.as<double>(), n, &c->status, ctx->stream));
@@ -1076,20 +1097,12 @@ int help_pcg_attach_mlp(help_pcg* ctx, help_mlp* mlp) {
     return HELP_OK;
 }
 
-int help_pcg_features(help_pcg* ctx, float* x) {
-    if (!ctx || !x) return HELP_E_ARG;
+int help_pcg_features(help_pcg* ctx, int32_t slot, float* x) {
+    if (!ctx || !x || slot < 0 || slot >= kSolveSlots) return HELP_E_ARG;
     if (!ctx->renewed) return fail(ctx, HELP_E_ARG, "features: renew first");
     CK(cudaSetDevice(ctx->device));
-    // features read D_S of the uncorrected preconditioner
-    double* saved = ctx->res.as<double>();
-    if (ctx->mlp_active) {
-        CK(cudaMemcpyAsync(saved, ctx->dsinv.p, 8 * (size_t)ctx->m, cudaMemcpyDeviceToDevice, ctx->stream));
-        CK(cudaMemcpyAsync(ctx->dsinv.p, ctx->dsinv_plain.p, 8 * (size_t)ctx->m, cudaMemcpyDeviceToDevice, ctx->stream));
-    }
-    int rc = learned_features(ctx, nullptr, x);
+    int rc = learned_features(ctx, slot, nullptr, x);
     if (rc) return rc;
-    if (ctx->mlp_active)
-        CK(cudaMemcpyAsync(ctx->dsinv.p, saved, 8 * (size_t)ctx->m, cudaMemcpyDeviceToDevice, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
     return HELP_OK;
 }

@@ -122,7 +122,8 @@ struct help_pcg {
     // of the current and the previous renew
     help_mlp* mlp = nullptr;
     bool mlp_active = false;          // correction applied in this renew (cleared by a fallback)
-    help::DevMem mlp_x, mlp_out, dsinv_plain;
+    help::DevMem mlp_x, mlp_out, dsinv_plain, d_prev;
+    bool have_dprev = false;          // d_prev holds the previous renew's d
     help::DevMem x2h[2][help::kSolveSlots];
     bool x2_have[2][help::kSolveSlots] = {};
     int x2_cur = 0;

@@ -11,24 +11,32 @@ namespace help {
 namespace {
 
 constexpr float kDiagClamp = 2.0f;  // |log-factor| of the D_S correction
+constexpr int kFeatures = 11;       // features in use; the rest of the row is zero
 
 // Writes the normalised BF16 row of X, or (X null) the raw FP32 row of R.
 __global__ void __launch_bounds__(256) k_features(const int* __restrict__ rp, const int* __restrict__ ci,
                                                   const double* __restrict__ d, const double* __restrict__ diag,
                                                   const double* __restrict__ dsinv, const int* __restrict__ pivpos,
-                                                  const double* __restrict__ xprev, const double* xprev_sumsq, int m,
+                                                  const double* __restrict__ xprev, const double* xprev_sumsq,
+                                                  const double* __restrict__ dprev, int m,
                                                   const MlpDevWeights* __restrict__ w, __nv_bfloat16* __restrict__ X,
                                                   float* __restrict__ R) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= m) return;
     const int b = rp[i], e = rp[i + 1];
-    float s = 0.f, s2 = 0.f, lo = 0.f, hi = 0.f;
+    float s = 0.f, s2 = 0.f, lo = 0.f, hi = 0.f, dm = 0.f, dx = 0.f;
     for (int q = b; q < e; ++q) {
-        const float l = log10f((float)d[ci[q]]);
+        const int j = ci[q];
+        const float l = log10f((float)d[j]);
         s += l;
         s2 += l * l;
         lo = (q == b) ? l : fminf(lo, l);
         hi = (q == b) ? l : fmaxf(hi, l);
+        if (dprev) {
+            const float c = l - log10f((float)dprev[j]);
+            dm += c;
+            dx = fmaxf(dx, fabsf(c));
+        }
     }
     const int len = e - b;
     const float mean = len > 0 ? s / len : 0.f;
@@ -51,8 +59,10 @@ __global__ void __launch_bounds__(256) k_features(const int* __restrict__ rp, co
         if (ss > 0.0) xf = (float)(xprev[i] / sqrt(ss / m));
     }
     f[8] = xf;
+    f[9] = len > 0 ? dm / len : 0.f;  // mean change of log10 d since the previous renew
+    f[10] = dx;                        // largest change
 #pragma unroll
-    for (int k = 9; k < HELP_MLP_IN; ++k) f[k] = 0.f;
+    for (int k = kFeatures; k < HELP_MLP_IN; ++k) f[k] = 0.f;
     if (!X) {
 #pragma unroll
         for (int k = 0; k < HELP_MLP_IN; ++k) R[(size_t)i * HELP_MLP_IN + k] = f[k];
@@ -61,8 +71,8 @@ __global__ void __launch_bounds__(256) k_features(const int* __restrict__ rp, co
     uint32_t* out = reinterpret_cast<uint32_t*>(X + (size_t)i * HELP_MLP_IN);
 #pragma unroll
     for (int k = 0; k < HELP_MLP_IN; k += 2) {
-        const float a = k < 9 ? (f[k] - w->mean[k]) * w->scale[k] : 0.f;
-        const float c = k + 1 < 9 ? (f[k + 1] - w->mean[k + 1]) * w->scale[k + 1] : 0.f;
+        const float a = k < kFeatures ? (f[k] - w->mean[k]) * w->scale[k] : 0.f;
+        const float c = k + 1 < kFeatures ? (f[k + 1] - w->mean[k + 1]) * w->scale[k + 1] : 0.f;
         const __nv_bfloat162 v = __floats2bfloat162_rn(a, c);
         out[k / 2] = *reinterpret_cast<const uint32_t*>(&v);
     }
@@ -87,10 +97,10 @@ __global__ void __launch_bounds__(256) k_warm_vector(const float* __restrict__ o
 }  // namespace
 
 cudaError_t mlp_features(const int* rp, const int* ci, const double* d, const double* diag, const double* dsinv,
-                         const int* pivpos, const double* xprev, const double* xprev_sumsq, int m,
-                         const MlpDevWeights* w, __nv_bfloat16* X, float* R, cudaStream_t st) {
+                         const int* pivpos, const double* xprev, const double* xprev_sumsq, const double* dprev,
+                         int m, const MlpDevWeights* w, __nv_bfloat16* X, float* R, cudaStream_t st) {
     if (m <= 0) return cudaSuccess;
-    k_features<<<(m + 255) / 256, 256, 0, st>>>(rp, ci, d, diag, dsinv, pivpos, xprev, xprev_sumsq, m, w, X, R);
+    k_features<<<(m + 255) / 256, 256, 0, st>>>(rp, ci, d, diag, dsinv, pivpos, xprev, xprev_sumsq, dprev, m, w, X, R);
     return cudaGetLastError();
 }
 

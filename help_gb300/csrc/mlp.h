@@ -54,11 +54,13 @@ cudaError_t mlp_upload(const float* prm, MlpDevWeights* w, cudaStream_t st);
 // Per-row features of the current renew, normalised, BF16 [m x HELP_MLP_IN]:
 //  0 log10 diag(G)_i   1..4 mean / std / min / max of log10 d_j over row i of A
 //  5 log2(1 + row length)   6 log10(D_S,i / diag_i) (0 on pivot rows)
-//  7 pivot flag   8 previous solution of solve slot 0, over its RMS (0 if none)
+//  7 pivot flag   8 this solve slot's solution in the previous renew, over
+//  its RMS (0 if none)   9 / 10 mean / largest |change| of log10 d over the
+//  row since the previous renew (0 if none)
 // With X null: the raw (unnormalised) FP32 features into R [m x HELP_MLP_IN].
 cudaError_t mlp_features(const int* rp, const int* ci, const double* d, const double* diag, const double* dsinv,
-                         const int* pivpos, const double* xprev, const double* xprev_sumsq, int m,
-                         const MlpDevWeights* w, __nv_bfloat16* X, float* R, cudaStream_t st);
+                         const int* pivpos, const double* xprev, const double* xprev_sumsq, const double* dprev,
+                         int m, const MlpDevWeights* w, __nv_bfloat16* X, float* R, cudaStream_t st);
 // dsinv_i *= exp(-clamp(out[i, 0])) on non-pivot rows (FP32 copy too when not null)
 cudaError_t mlp_apply_diag(const float* out, const int* pivpos, double* dsinv, float* dsinv32, int m,
                            cudaStream_t st);

@@ -4,8 +4,8 @@ warm-start scale for the normal-equations PCG (include/help_gpu.h, HELP_MLP_*).
 Pipeline, all on the GPU through the library's own kernels:
   1. ``collect``: run the HSD interior-point method with the plain FP64 PCG
      backend on seeded LPs; after every renew record the raw per-row features
-     (device kernel, help_pcg_features), the pivots and the solutions x_2 of
-     every solve slot;
+     of every solve slot (device kernel, help_pcg_features), the pivots and
+     the solutions x_2 of every solve slot;
   2. ``targets``: per row, (0) the log-ratio of a 2-norm equilibrated diagonal
      of the Schur complement S (non-pivot block) to diag(S) -- computed from
      the dense S, so for small systems only -- and (1) the per-row scale s of
@@ -28,6 +28,10 @@ import numpy as np
 
 from . import native
 from .backend import GpuNormalEquations
+
+
+FEATURES = 11   # features in use per row (include/help_gpu.h); the rest of the 16 are zero
+SLOTS = 4       # solve slots after a renew that get their own features
 
 
 def _torch():
@@ -184,13 +188,15 @@ class _Recorder:
 
     def _snapshot(self, d_ptr) -> None:
         ne = self.ne
-        rc = ne.lib.help_pcg_features(ne.ctx, self._feat.data_ptr())
-        if rc != native.HELP_OK:
-            raise RuntimeError("help_pcg_features failed (%d)" % rc)
+        feats = []
+        for slot in range(SLOTS):
+            rc = ne.lib.help_pcg_features(ne.ctx, slot, self._feat.data_ptr())
+            if rc != native.HELP_OK:
+                raise RuntimeError("help_pcg_features failed (%d)" % rc)
+            feats.append(self._feat.cpu().numpy().copy())
         piv, dg, ds = ne.pivots()
         d = np.ctypeslib.as_array(C.cast(d_ptr, C.POINTER(C.c_double)), (self.n,)).copy()
-        self.renews.append({"feat": self._feat.cpu().numpy().copy(), "piv": piv.copy(), "diag": dg.copy(),
-                            "ds": ds.copy(), "d": d, "x2": []})
+        self.renews.append({"feat": feats, "piv": piv.copy(), "diag": dg.copy(), "ds": ds.copy(), "d": d, "x2": []})
 
     def backend(self) -> native.NeBackend:
         f = lambda fn: C.cast(fn, C.c_void_p).value
@@ -286,7 +292,7 @@ def targets(lp, renews: list[dict], dense_max: int = 4000, diag: bool = True) ->
             t = np.stack([t0, t1], 1)
             w0 = mask / max(len(N), 1) if (s == 0 and diag) else np.zeros(lp.m)
             w = np.stack([w0, np.full(lp.m, 1.0 / lp.m)], 1)
-            X.append(cur["feat"])
+            X.append(cur["feat"][min(s, SLOTS - 1)])
             T.append(t)
             W.append(w)
     return {"X": np.concatenate(X).astype(np.float32), "T": np.concatenate(T).astype(np.float32),
@@ -296,16 +302,16 @@ def targets(lp, renews: list[dict], dense_max: int = 4000, diag: bool = True) ->
 def normalisation(X: np.ndarray) -> tuple[np.ndarray, np.ndarray]:
     mean = np.zeros(native.MLP_IN, np.float32)
     scale = np.ones(native.MLP_IN, np.float32)
-    mean[:9] = X[:, :9].mean(0)
-    sd = X[:, :9].std(0)
-    scale[:9] = np.where(sd > 1e-6, 1.0 / np.maximum(sd, 1e-6), 1.0)
+    mean[:FEATURES] = X[:, :FEATURES].mean(0)
+    sd = X[:, :FEATURES].std(0)
+    scale[:FEATURES] = np.where(sd > 1e-6, 1.0 / np.maximum(sd, 1e-6), 1.0)
     return mean, scale
 
 
 def normalise_bits(X: np.ndarray, mean: np.ndarray, scale: np.ndarray) -> np.ndarray:
     """The device feature kernel's normalisation and BF16 rounding, on the host."""
     Z = ((X.astype(np.float32) - mean) * scale).astype(np.float32)
-    Z[:, 9:] = 0.0
+    Z[:, FEATURES:] = 0.0
     return bf16_bits(Z)
 
 

@@ -233,7 +233,7 @@ def gpu_lib() -> C.CDLL:
         lib.help_mlp_loss_grad.argtypes = [vp, vp, vp, vp, i64, C.POINTER(C.c_double), dp]
         lib.help_mlp_train_step.argtypes = [vp, vp, vp, vp, i64, C.c_float, C.POINTER(C.c_double)]
         lib.help_pcg_attach_mlp.argtypes = [vp, vp]
-        lib.help_pcg_features.argtypes = [vp, vp]
+        lib.help_pcg_features.argtypes = [vp, C.c_int32, vp]
         for s in GPU_SYMBOLS:
             getattr(lib, s)
         _gpu = lib

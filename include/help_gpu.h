@@ -175,7 +175,9 @@ int help_adat_assemble(help_pcg* ctx, const double* w, int32_t* row_ptr, int32_t
  * Features (row i of A, d = D):  0 log10 diag(A D^-1 A^T)_ii,  1-4 mean /
  * std / min / max of log10 d_j over the row,  5 log2(1 + row length),
  * 6 log10(D_S,i / diag_i) (0 on pivot rows),  7 pivot flag,  8 x_2 of the
- * previous renew's first solve over its RMS;  9-15 zero.  Each is normalised
+ * same solve slot in the previous renew over its RMS,  9 / 10 mean /
+ * largest |change| of log10 d_j over the row since the previous renew;
+ * 11-15 zero.  Solve slot s > 0 runs the model on its own features.  Each is normalised
  * as (f - mean) * scale with the model's constants, then rounded to BF16.
  *
  * Parameters (FP32, HELP_MLP_PARAMS floats): W1[64][16], b1[64], W2[64][64],
@@ -213,10 +215,11 @@ int help_mlp_train_step(help_mlp* mlp, const void* x, const float* target, const
 /* Use `mlp` in this context's solves from the next renew on (NULL: plain PCG).
  * The model must live on the context's device and outlive the attachment. */
 int help_pcg_attach_mlp(help_pcg* ctx, help_mlp* mlp);
-/* Raw (unnormalised) FP32 features of the current renew into the device
- * array x [m][16]; the previous renew's first solution is used when a model
- * was attached during it. */
-int help_pcg_features(help_pcg* ctx, float* x);
+/* Raw (unnormalised) FP32 features of the current renew for solve slot
+ * `slot` (0 .. 3, the order of the solves after a renew) into the device
+ * array x [m][16]; the previous renew's solution of that slot and its d are
+ * used when a model was attached during it. */
+int help_pcg_features(help_pcg* ctx, int32_t slot, float* x);
 
 /* ---- no-allocation product (no counterpart in the reference) ----
  *

@@ -50,6 +50,6 @@ def test_feature_bits_round_to_nearest_even():
     scale = np.linspace(0.5, 2, 16).astype(np.float32)
     bits = learned.normalise_bits(x, mean, scale)
     z = (x - mean) * scale
-    z[:, 9:] = 0
+    z[:, learned.FEATURES:] = 0
     ref = torch.from_numpy(z).to(torch.bfloat16).view(torch.int16).numpy().view(np.uint16)
     assert np.array_equal(bits, ref)
