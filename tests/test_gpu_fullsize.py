@@ -1,0 +1,85 @@
+"""The benchmark's configurations at full size, through properties that hold
+whatever the size (the oracle is too slow there):
+
+  * G = A D^-1 A^T is symmetric:      x . G y == y . G x
+  * and linear:                      G (a x + b y) == a G x + b G y
+  * the fused product equals A (D^-1 (A^T x)) from the separate A^T and A
+    products (the reference's CSRMV_T, scale, CSRMV_N order)
+  * FP32 copies agree with FP64 to FP32 accuracy
+  * the preconditioner is symmetric and positive: r . M^-1 s == s . M^-1 r,
+    r . M^-1 r > 0
+  * CG lowers the energy 1/2 x.Gx - b.x below its value at x = 0 (the
+    quantity CG minimises; the residual's 2-norm need not fall)
+
+Tolerances: 1e-12 relative for FP64 identities (sums of up to ~10^5 terms
+per row in different orders), 1e-5 for FP32 against FP64.
+"""
+import numpy as np
+import pytest
+
+from help_gb300 import backend, lp as L
+
+pytestmark = pytest.mark.gpu
+
+
+def rel(a, b):
+    return np.linalg.norm(np.asarray(a) - np.asarray(b)) / max(np.linalg.norm(b), 1e-300)
+
+
+@pytest.fixture(scope="module", params=[1, 2, 3, 4])
+def system(request):
+    config = request.param
+    lp = L.make_lp(config, 0)
+    rng = np.random.default_rng(100 + config)
+    d = np.exp(rng.uniform(np.log(1e-8), np.log(1e8), lp.n))
+    k = L.config_pivots(config)
+    g = backend.GpuNormalEquations(pivots=k, precision="mixed", cg_tol=1e-6, cg_max_iter=200)
+    g.LinearEquation_Construct(lp)
+    g.RenewLinearEquation(d)
+    yield config, lp, d, g, rng
+    g.close()
+
+
+def test_product_symmetric_and_linear(system):
+    config, lp, d, g, rng = system
+    x, y = rng.standard_normal(lp.m), rng.standard_normal(lp.m)
+    gx, gy = g.matvec("ADAT", x), g.matvec("ADAT", y)
+    assert abs(x @ gy - y @ gx) <= 1e-12 * np.linalg.norm(x) * np.linalg.norm(gy)
+    a, b = 0.75, -1.5
+    assert rel(g.matvec("ADAT", a * x + b * y), a * gx + b * gy) < 1e-12
+
+
+def test_fused_product_matches_separate_passes(system):
+    config, lp, d, g, rng = system
+    x = rng.standard_normal(lp.m)
+    t = g.matvec("AT", x) / d
+    assert rel(g.matvec("ADAT", x), g.matvec("A", t)) < 1e-12
+
+
+def test_fp32_copy_agrees_with_fp64(system):
+    torch = pytest.importorskip("torch")
+    config, lp, d, g, rng = system
+    x = rng.standard_normal(lp.m)
+    y64 = g.matvec("ADAT", x)
+    x32 = torch.from_numpy(x.astype(np.float32)).cuda()
+    y32 = torch.empty(lp.m, dtype=torch.float32, device="cuda")
+    g.matvec_dev("ADAT", x32.data_ptr(), y32.data_ptr(), fp32=True)
+    torch.cuda.synchronize()
+    assert rel(y32.cpu().numpy().astype(np.float64), y64) < 1e-5
+
+
+def test_preconditioner_symmetric_positive(system):
+    config, lp, d, g, rng = system
+    r, s = rng.standard_normal(lp.m), rng.standard_normal(lp.m)
+    mr, ms = g.precond_apply(r), g.precond_apply(s)
+    assert abs(r @ ms - s @ mr) <= 1e-9 * np.linalg.norm(r) * np.linalg.norm(ms)
+    assert r @ mr > 0 and s @ ms > 0
+
+
+def test_cg_lowers_the_energy(system):
+    config, lp, d, g, rng = system
+    b = rng.standard_normal(lp.m)
+    x, it = g.cg(b)
+    assert it > 0
+    energy = 0.5 * (x @ g.matvec("ADAT", x)) - b @ x
+    assert energy < 0.0
