@@ -558,7 +558,9 @@ int renew_impl(help_pcg* ctx, const double* d_host) {
     CK(renew_scale_values(ctx->s.as<double>(), ctx->rp.as<int>(), ctx->ci.as<int>(), ctx->av.as<double>(),
                           ctx->bv.as<double>(), mixed ? ctx->bv32.as<float>() : nullptr, ctx->cp.as<int>(),
                           ctx->avT.as<double>(), ctx->bvT.as<double>(), mixed ? ctx->bvT32.as<float>() : nullptr,
-                          ctx->diag.as<double>(), ctx->opt.delta, m, n, ctx->nnz, ctx->stream));
+                          ctx->diag.as<double>(), ctx->opt.delta, m, n, ctx->nnz, &c->status, ctx->stream));
+    rc = read_status(ctx, "renew: a row of A has no nonzeros, so A D^-1 A^T is singular (remove the row or set delta > 0)");
+    if (rc) return rc;
     // pivots
     const int k = std::max(0, std::min(ctx->opt.pivots, m));
     ctx->k = k;

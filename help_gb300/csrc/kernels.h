@@ -107,10 +107,10 @@ cudaError_t vec_scale(double* x, double a, int64_t n, cudaStream_t st);
 // s = d^-1/2 (status <- numeric error if some d_j is not positive and finite)
 cudaError_t renew_inv_sqrt(const double* d, double* s, int n, int* status, cudaStream_t st);
 // B = A diag(s) in both layouts (FP32 copies when bv32 / bvT32 are not null)
-// and diag = rowsum(B .* B) + delta.
+// and diag = rowsum(B .* B) + delta (status <- numeric error if some diag <= 0).
 cudaError_t renew_scale_values(const double* s, const int* rp, const int* ci, const double* av, double* bv,
                                float* bv32, const int* cp, const double* avT, double* bvT, float* bvT32,
-                               double* diag, double delta, int m, int n, int64_t nnz, cudaStream_t st);
+                               double* diag, double delta, int m, int n, int64_t nnz, int* status, cudaStream_t st);
 // Top-k rows by key (diag >= 0); pivots ascending in piv[0..k), pivpos[m] = position or -1.
 // flags: 3*m ints of scratch.
 cudaError_t topk_select(const double* diag, int m, int k, unsigned long long* keys, unsigned int* hist,

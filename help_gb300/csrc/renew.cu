@@ -67,12 +67,16 @@ __global__ void k_scale_cols(const int* __restrict__ cp, const double* __restric
 }
 
 // diag[i] = sum_e bv[e]^2 + delta (thread per row, FMA in column order)
+// diag(G) = rowsum(B .* B) + delta; status <- numeric error where a diagonal
+// is not positive (a row of A without nonzeros and delta = 0: G is singular)
 __global__ void k_row_sumsq(const int* __restrict__ rp, const double* __restrict__ bv, double* __restrict__ diag,
-                            double delta, int m) {
+                            double delta, int m, int* __restrict__ status) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < m; i += (int64_t)gridDim.x * blockDim.x) {
         double acc = 0.0;
         for (int e = rp[i]; e < rp[i + 1]; ++e) acc = fma(bv[e], bv[e], acc);
-        diag[i] = acc + delta;
+        const double g = acc + delta;
+        diag[i] = g;
+        if (!(g > 0.0)) atomicExch(status, kStatusNumeric);
     }
 }
 
@@ -447,10 +451,10 @@ cudaError_t renew_inv_sqrt(const double* d, double* s, int n, int* status, cudaS
 
 cudaError_t renew_scale_values(const double* s, const int* rp, const int* ci, const double* av, double* bv,
                                float* bv32, const int* cp, const double* avT, double* bvT, float* bvT32,
-                               double* diag, double delta, int m, int n, int64_t nnz, cudaStream_t st) {
+                               double* diag, double delta, int m, int n, int64_t nnz, int* status, cudaStream_t st) {
     k_scale_elems<<<grid_for(nnz, 256), 256, 0, st>>>(ci, av, s, bv, bv32, nnz);
     k_scale_cols<<<grid_for(n, 128), 128, 0, st>>>(cp, avT, s, bvT, bvT32, n);
-    k_row_sumsq<<<grid_for(m, 128), 128, 0, st>>>(rp, bv, diag, delta, m);
+    k_row_sumsq<<<grid_for(m, 128), 128, 0, st>>>(rp, bv, diag, delta, m, status);
     return cudaGetLastError();
 }
 
