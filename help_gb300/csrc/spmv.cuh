@@ -23,7 +23,7 @@
 // Loads go through L1 (read-only path) so the neighbouring elements a group
 // reads next reuse the sectors already fetched.  All loops are grid-stride
 // over every warp / block of the launch, so the same routine serves the
-// standalone kernels and the phases of the persistent CG kernel.  One FMA per
+// standalone kernels, the CG graph kernels and the single-cluster CG kernel.  One FMA per
 // nonzero and few shuffle adds matter on GB300, whose FP64 rate (~2
 // DFMA/clk/SM) is close to the HBM rate for SpMV.
 #pragma once

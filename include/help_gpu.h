@@ -59,9 +59,11 @@ typedef struct help_pcg_options {
     int32_t ir_max_outer;    /* refinement steps before falling back to FP64 PCG        */
     double inner_tol;        /* relative residual reduction asked of each FP32 CG run   */
     int64_t inner_max_iter;  /* cap per FP32 CG run                                     */
-    /* warm start / learned correction */
+    /* warm start and fallback (the learned correction is attached separately,
+       help_pcg_attach_mlp, and brings its own warm start) */
     int32_t warm_start;      /* 1: start CG from the previous solve's x_2 of this renew */
-    int32_t fallback;        /* 1: on cap or failed FP64 check, redo with plain FP64 PCG */
+    int32_t fallback;        /* 1: mixed form -- when FP32 refinement stalls or hits its
+                                cap, finish with plain FP64 PCG                          */
     int32_t cg_path;         /* 0 auto: one thread-block cluster runs whole CG iterations
                                 when the system is small, else the multi-kernel graph;
                                 1 always the graph; 2 always the cluster kernel          */
