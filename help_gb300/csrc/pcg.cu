@@ -162,16 +162,18 @@ __global__ void __launch_bounds__(kCgThreads) k_p3(const CgArgs<V> A) {
         A.ct, [&](int i) { return A.z[i]; },
         [&](int c, V s) { A.w[c] = (double)r[A.piv[c]] - (double)s; }, red);
     if (publish_partial(0.0, A.part_aw, &A.sc->ticket[1])) {
-        // every block has written its w entries: r_P . z_P = a . w over all k
-        // in order, plus the r.z terms of C's long rows, plus k_p2's partials
-        // (same grid)
-        double aw = 0.0;
-        for (int c = threadIdx.x; c < A.k; c += blockDim.x) aw = fma(A.a[c], __ldcg(A.w + c), aw);
-        aw = block_sum(aw, red);
-        const double rzl = long_rows_sum(
-            A.c,
-            [&](int i) { return A.pivpos[i] < 0 ? (double)__ldcg(r + i) * (double)__ldcg(A.z + i) : 0.0; }, red);
-        const double rz = sum_parts(A.part_rz, nullptr, gridDim.x, red) + rzl + aw;
+        // every block has written its w entries.  rz = k_p2's partials (same
+        // grid) + a . w over all k (= r_P . z_P) + the r.z terms of C's long
+        // rows: each thread sums its share of the three in a fixed order, then
+        // one block reduction
+        double acc = 0.0;
+        for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x) acc += A.part_rz[b];
+        for (int c = threadIdx.x; c < A.k; c += blockDim.x) acc = fma(A.a[c], __ldcg(A.w + c), acc);
+        for (int j = threadIdx.x; j < A.c.n_long; j += blockDim.x) {
+            const int i = A.c.long_rows[j];
+            if (A.pivpos[i] < 0) acc = fma((double)__ldcg(r + i), (double)__ldcg(A.z + i), acc);
+        }
+        const double rz = block_sum(acc, red);
         if (threadIdx.x == 0) {
             CgScalars* sc = A.sc;
             sc->ticket[1] = 0;
@@ -241,9 +243,13 @@ __global__ void __launch_bounds__(kCgThreads) k_b(const CgArgs<V> A) {
         [&](int i, V s) { A.q[i] = has_delta ? fma_t(vd, pn[i], s) : s; }, red);
     pq = block_sum(pq, red);
     if (publish_partial(pq, A.part_pq, &A.sc->ticket[2])) {
-        const double pql = long_rows_sum(
-            A.csr, [&](int i) { return (double)__ldcg(pn + i) * (double)__ldcg(A.q + i); }, red);
-        const double tot = sum_parts(A.part_pq, nullptr, gridDim.x, red) + pql;
+        double acc = 0.0;
+        for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x) acc += __ldcg(A.part_pq + b);
+        for (int j = threadIdx.x; j < A.csr.n_long; j += blockDim.x) {
+            const int i = A.csr.long_rows[j];
+            acc = fma((double)__ldcg(pn + i), (double)__ldcg(A.q + i), acc);
+        }
+        const double tot = block_sum(acc, red);
         if (threadIdx.x == 0) {
             CgScalars* sc = A.sc;
             sc->ticket[2] = 0;
@@ -399,14 +405,14 @@ __global__ void __launch_bounds__(kClusterThreads) k_cg_cluster(const CgArgs<V> 
         cl.sync();
         {
             // a . w over all k and the long rows' r.z terms, the same in every CTA
-            double aw = 0.0;
-            for (int c = tid; c < A.k; c += blockDim.x) aw = fma(__ldcg(A.a + c), __ldcg(A.w + c), aw);
-            aw = block_sum(aw, red);
-            const double rzl = long_rows_sum(
-                A.c,
-                [&](int i) { return A.pivpos[i] < 0 ? (double)__ldcg(r + i) * (double)__ldcg(A.z + i) : 0.0; },
-                red);
-            rz = cluster_total(cl, s_part, 0, -1, &s_tot[0]) + rzl + aw;
+            double acc = 0.0;
+            for (int c = tid; c < A.k; c += blockDim.x) acc = fma(__ldcg(A.a + c), __ldcg(A.w + c), acc);
+            for (int j = tid; j < A.c.n_long; j += blockDim.x) {
+                const int i = A.c.long_rows[j];
+                if (A.pivpos[i] < 0) acc = fma((double)__ldcg(r + i), (double)__ldcg(A.z + i), acc);
+            }
+            const double own = block_sum(acc, red);
+            rz = cluster_total(cl, s_part, 0, -1, &s_tot[0]) + own;
         }
         if (!(rz > 0.0)) {
             done = 3;
