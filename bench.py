@@ -192,7 +192,7 @@ def ipm_run(config: int, precision: str, pivots: int | None = None) -> dict:
     return {"config": "config %d: m=%d n=%d nnz=%d" % (config, lp.m, lp.n, lp.nnz),
             "form": "%s PCG, k=%d, tol 1e-10, CG path %s" % (
                 "plain FP64" if precision == "fp64" else "FP32 CG in FP64 refinement", k,
-                {1: "graph", 2: "single cluster"}.get(int(st["cg_path_used"]), "?")),
+                {1: "graph", 2: "single cluster", 3: "resident cluster"}.get(int(st["cg_path_used"]), "?")),
             "seconds": round(wall, 3), "status": r["status"], "iterations": r["iterations"],
             "rel_gap": r["rel_gap"], "primal_obj": r["primal_obj"], "primal_infeas": r["primal_infeas"],
             "dual_infeas": r["dual_infeas"], "cg_iterations": int(st["cg_iterations_total"]),
@@ -285,7 +285,7 @@ def pcg_rate(config: int, iters: int, local: int) -> dict:
             out[prec] = {"iterations": int(it), "us_per_iteration": round(us, 2), "iterations_per_s": round(1e6 / us, 1)}
     out.update({"workload": "config %d: m=%d n=%d nnz=%d, k=%d, nnz(C)=%d" % (config, lp.m, lp.n, lp.nnz, k, st["nnz_c"]),
                 "renew_ms": round(renew_ms, 2),
-                "path": {1: "graph", 2: "single cluster"}.get(int(st["cg_path_used"]), "?")})
+                "path": {1: "graph", 2: "single cluster", 3: "resident cluster"}.get(int(st["cg_path_used"]), "?")})
     return out
 
 

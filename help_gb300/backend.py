@@ -64,7 +64,7 @@ class GpuNormalEquations:
         o.inner_max_iter = int(inner_max_iter)
         o.warm_start = int(bool(warm_start))
         o.fallback = int(bool(fallback))
-        o.cg_path = {"auto": 0, "graph": 1, "cluster": 2}[cg_path]
+        o.cg_path = {"auto": 0, "graph": 1, "cluster": 2, "resident": 3}[cg_path]
         self.options = o
         h = C.c_void_p()
         self._check(self.lib.help_pcg_create(C.byref(o), C.byref(h)), None)

@@ -26,7 +26,7 @@ NVCC = os.environ.get("NVCC", "nvcc")
 CXX = os.environ.get("CXX", "g++")
 GENCODE = "-gencode=arch=compute_103a,code=sm_103a"
 
-GPU_CU = ["api.cu", "pcg.cu", "renew.cu", "dense.cu", "vec.cu", "adat.cu", "noalloc.cu", "mlp.cu",
+GPU_CU = ["api.cu", "pcg.cu", "pcg_resident.cu", "renew.cu", "dense.cu", "vec.cu", "adat.cu", "noalloc.cu", "mlp.cu",
           "learned.cu", "mlp_api.cu"]
 GPU_CPP = ["items.cpp"]
 GPU_HDR = ["common.cuh", "spmv.cuh", "kernels.h", "context.h", "items.h", "mlp.h"]

@@ -161,6 +161,18 @@ int64_t cluster_work(const help_pcg* ctx) {
     return 2 * (ctx->nnz + ctx->nnz_c) + 8 * (int64_t)ctx->m + (int64_t)ctx->k * ctx->k;
 }
 
+// Cluster size of the shared-memory-resident CG for this precision, or 0
+// when it does not apply: vectors too large, too many pivots, or a row of B
+// or B^T longer than 32 G nonzeros (those rows need a warp or CTA each).
+int resident_fits(const help_pcg* ctx, bool f32) {
+    const int slot = f32 ? 1 : 0;
+    if (ctx->resident_cs[slot] <= 0) return 0;
+    const RowSplit& a = f32 ? ctx->pl_csr.s32 : ctx->pl_csr.s64;
+    const RowSplit& b = f32 ? ctx->pl_csc.s32 : ctx->pl_csc.s64;
+    if (a.n_med + a.n_long + b.n_med + b.n_long != 0) return 0;
+    return ctx->resident_cs[slot];
+}
+
 int finish_pcg(help_pcg* ctx, bool f32, const CgScalars* h, CgResult* res) {
     CK(cudaEventSynchronize(ctx->ev1));
     float kms = 0.f;
@@ -221,12 +233,30 @@ int run_pcg(help_pcg* ctx, V* x, V* r0, double tol, long long max_iter, int prec
     h->max_iter = max_iter;
     CK(cudaMemcpyAsync(&c->cg, h, sizeof(CgScalars), cudaMemcpyHostToDevice, ctx->stream));
     const int cs = ctx->cluster_cs[slot];
-    bool cluster = false;
-    if (!precond_only && cs > 0) {
-        if (ctx->opt.cg_path == 2) cluster = true;
-        else if (ctx->opt.cg_path == 0) cluster = cluster_work(ctx) <= kClusterWorkMax;
+    bool cluster = false, resident = false;
+    if (!precond_only) {
+        const int rcs = resident_fits(ctx, f32);
+        if (rcs > 0 && (ctx->opt.cg_path == 0 || ctx->opt.cg_path == 3)) resident = true;
+        else if (cs > 0 && ctx->opt.cg_path == 2) cluster = true;
+        else if (cs > 0 && (ctx->opt.cg_path == 0 || ctx->opt.cg_path == 3))
+            cluster = cluster_work(ctx) <= kClusterWorkMax;
     }
-    ctx->stats.cg_path_used = cluster ? 2 : 1;
+    ctx->stats.cg_path_used = resident ? 3 : cluster ? 2 : 1;
+    if (resident) {
+        const int rcs = ctx->resident_cs[slot];
+        CK(cudaEventRecord(ctx->ev0, ctx->stream));
+        CK(cg_launch_init<V>(A, nb, ctx->stream));
+        int per = 64;
+        for (;;) {
+            CK(cg_launch_resident<V>(A, ctx->resident_layout[slot], rcs, per, ctx->stream));
+            CK(cudaMemcpyAsync(h, &c->cg, sizeof(CgScalars), cudaMemcpyDeviceToHost, ctx->stream));
+            CK(cudaStreamSynchronize(ctx->stream));
+            if (h->done != 0) break;
+            per = std::min(per * 2, 4096);
+        }
+        CK(cudaEventRecord(ctx->ev1, ctx->stream));
+        return finish_pcg(ctx, f32, h, res);
+    }
     if (cluster) {
         CK(cudaEventRecord(ctx->ev0, ctx->stream));
         CK(cg_launch_init<V>(A, nb, ctx->stream));
@@ -641,6 +671,12 @@ int renew_impl(help_pcg* ctx, const double* d_host) {
     }
     rc = upload_plan(ctx, ctx->pl_ct, ctp.data(), k, mixed);
     if (rc) return rc;
+    // shared-memory-resident CG: layout for this renew's C (h_tmp = C's row pointers)
+    ctx->resident_cs[0] = cg_resident_configure<double>(m, n, k, ctx->h_rp.data(), ctx->h_cp.data(),
+                                                        ctx->h_tmp.data(), &ctx->resident_layout[0]);
+    ctx->resident_cs[1] = mixed ? cg_resident_configure<float>(m, n, k, ctx->h_rp.data(), ctx->h_cp.data(),
+                                                               ctx->h_tmp.data(), &ctx->resident_layout[1])
+                                : 0;
     // pivot block inverse and the Schur diagonal
     CK(cudaMemsetAsync(&c->regularised, 0, sizeof(int), ctx->stream));
     if (k > 0)

@@ -135,6 +135,8 @@ struct help_pcg {
     std::vector<unsigned char> graph_args[2];
     int cg_blocks = 0;
     int cluster_cs[2] = {0, 0};       // single-cluster CG: CTAs per cluster (0 = unavailable)
+    int resident_cs[2] = {0, 0};      // shared-memory-resident CG (set at renew): CTAs per cluster, 0 = no fit
+    help::ResLayout resident_layout[2] = {};
     help::DevMem cg_part;  // 4 x cg_blocks doubles
     help::CgScalars* h_sc = nullptr;  // pinned mirror of the device scalars
     double solve_kernel_ms = 0;       // accumulators for the current solve

@@ -77,6 +77,24 @@ int cg_cluster_configure(int k_max);
 template <class V>
 cudaError_t cg_launch_cluster(const CgArgs<V>& A, int cs, int iters, cudaStream_t st);
 
+// Single-cluster CG with the vectors and the matrix slices in shared memory
+// (pcg_resident.cu), for systems with at most kResidentMaxPivots pivots whose
+// rows of B and B^T all hold <= 32 G nonzeros.  Byte offsets into the
+// kernel's dynamic shared memory; lr / lc rows / columns per CTA.
+constexpr int kResidentMaxPivots = 64;
+struct ResLayout {
+    int lr, lc;
+    size_t a, w, kpart, s_rz, s_rr, s_pq, W, pf, tf, xl, rl, zl, ql, dl, rp, qp, pvl, piv, ct_p, ct_b, ct_i, ct_v,
+        csr_p, csr_i, csr_v, csc_p, csc_i, csc_v, c_p, c_i, c_v, total;
+};
+ResLayout resident_layout(int m, int n, int k, int cs, int vbytes, const int32_t* rp, const int32_t* cp,
+                          const int32_t* crp);
+template <class V>
+int cg_resident_configure(int m, int n, int k, const int32_t* rp, const int32_t* cp, const int32_t* crp,
+                          ResLayout* L);
+template <class V>
+cudaError_t cg_launch_resident(const CgArgs<V>& A, const ResLayout& L, int cs, int iters, cudaStream_t st);
+
 // ---- standalone SpMV over items (vec.cu)
 enum SpmvEpi {
     kEpiStore = 0,     // y[row] = s

@@ -1,0 +1,553 @@
+// Single-cluster CG with every vector resident in shared memory -- the loop
+// of ConjugateGradient (PCG.cpp:296-395) and the block-form preconditioner
+// of PCG.cpp:183-196 for systems whose vectors fit on one cluster's SMs.
+//
+// A cluster of 16 (or 8) CTAs, one per SM, owns the solve.  CTA c owns a
+// contiguous slice of the rows of G (m) and of the columns of A (n).  Every
+// CTA keeps in its shared memory
+//   * full copies of p (m) and t = B^T p (n), the two gathered vectors;
+//   * its own slices of x, r, z, q;
+//   * the pivot-row values r_P, q_P, a = W r_P and w (k each), replicated.
+// and its slices of the matrix (its rows of B, C and D_S^-1, its columns of B
+// -- rows of B^T --, its entries of C^T, and W), copied from HBM once per
+// launch: the acquire side of every cluster barrier invalidates L1, so a
+// matrix read through L1 would come back from L2 after each barrier.  Each
+// iteration is four steps separated by hardware cluster barriers
+// (barrier.cluster arrive.release / wait.acquire); a CTA hands its results to
+// the others by plain stores into their shared memory (DSMEM) before the
+// barrier, so no CTA ever reads a remote SM and nothing but the launch's
+// first and last copies touches HBM or L2:
+//   (i)   z_N = D_S^-1 (r_N - C a) on own rows; r_N.z_N and the k-vector
+//         C^T z_N over own rows -> every CTA
+//         -- barrier --  stop test on r.r of the previous step (iv)
+//   (ii)  w = r_P - sum C^T z_N, rz = r_N.z_N + a.w, beta, z_P = W w on own
+//         pivot rows, p = z + beta p on own rows -> every CTA's p
+//         -- barrier --
+//   (iii) t = B^T p on own columns -> every CTA's t
+//         -- barrier --
+//   (iv)  q = B t + delta p on own rows; p.q and q_P -> every CTA
+//         -- barrier --  alpha; x += alpha p, r -= alpha q on own rows, r.r
+//         -> every CTA; r_P -= alpha q_P and a = W r_P in every CTA
+// Every CTA adds the CTAs' partials in rank order, so all of them form
+// bit-identical alpha, beta and stopping decisions and leave the loop
+// together.  Row sums use the same lane groups and shuffle order as the
+// whole-GPU kernels (spmv.cuh) for rows of up to 32 G nonzeros, the only
+// rows this path accepts.
+#include <cooperative_groups.h>
+
+#include <algorithm>
+
+#include "common.cuh"
+#include "kernels.h"
+#include "spmv.cuh"
+
+namespace cg = cooperative_groups;
+
+namespace help {
+
+namespace {
+
+constexpr int kResThreads = 256;
+constexpr int kResWarps = kResThreads / 32;
+
+// A CSR slice in shared memory: rows 0..rows-1 (row0 + r in the whole
+// matrix), ptr rebased to 0, column indices of the whole matrix.
+template <class V>
+struct LocalCsr {
+    const int* ptr;
+    const int* idx;
+    const V* val;
+    int rows, row0, G;
+};
+
+// ep(row0 + r, sum) once per row by the group's first lane; G lanes per row.
+template <class V, class XF, class EP>
+HELP_DEVINL void rows_local(const LocalCsr<V>& M, const XF& xf, const EP& ep) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int G = M.G, lg = __ffs(G) - 1;
+    const int sub = lane & (G - 1), rpw = 32 >> lg;
+    for (int base = warp * rpw; base < M.rows; base += kResWarps * rpw) {
+        const int row = base + (lane >> lg);
+        int b = 0, e = 0;
+        if (row < M.rows) {
+            b = M.ptr[row];
+            e = M.ptr[row + 1];
+        }
+        V acc = V(0);
+        int q = b + sub;
+        for (; q + 3 * G < e; q += 4 * G) {
+            const int c0 = M.idx[q], c1 = M.idx[q + G];
+            const int c2 = M.idx[q + 2 * G], c3 = M.idx[q + 3 * G];
+            const V v0 = M.val[q], v1 = M.val[q + G];
+            const V v2 = M.val[q + 2 * G], v3 = M.val[q + 3 * G];
+            const V x0 = xf(c0), x1 = xf(c1), x2 = xf(c2), x3 = xf(c3);
+            acc = fma_t(v0, x0, acc);
+            acc = fma_t(v1, x1, acc);
+            acc = fma_t(v2, x2, acc);
+            acc = fma_t(v3, x3, acc);
+        }
+        for (; q < e; q += G) acc = fma_t(M.val[q], xf(M.idx[q]), acc);
+        for (int o = G >> 1; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+        if (row < M.rows && sub == 0) ep(M.row0 + row, acc);
+    }
+}
+
+// Copies rows [lo, hi) of a CSR matrix in HBM into shared memory (pointers
+// rebased to 0); returns the slice.
+template <class V>
+HELP_DEVINL LocalCsr<V> load_rows(const SpmvView<V>& M, int lo, int hi, int* sp, int* si, V* sv) {
+    const int b = ld_ro(M.ptr + lo);
+    for (int r = threadIdx.x; r <= hi - lo; r += kResThreads) sp[r] = ld_ro(M.ptr + lo + r) - b;
+    const int e = ld_ro(M.ptr + hi);
+    for (int q = threadIdx.x; q < e - b; q += kResThreads) {
+        si[q] = ld_ro(M.idx + b + q);
+        sv[q] = ld_ro(M.val + b + q);
+    }
+    LocalCsr<V> L;
+    L.ptr = sp;
+    L.idx = si;
+    L.val = sv;
+    L.rows = hi - lo;
+    L.row0 = lo;
+    L.G = M.G;
+    return L;
+}
+
+// Copies buf[lo, hi) of this CTA into the same range of every other CTA's
+// buf.  lo * sizeof(V) and buf are 16-byte aligned (slices start at multiples
+// of 4 elements), so the body moves 16-byte words.
+template <class V>
+HELP_DEVINL void push_slice(cg::cluster_group& cl, V* buf, int lo, int hi, int rank, int cs) {
+    if (hi <= lo) return;
+    const int nb = (hi - lo) * (int)sizeof(V);
+    const int n16 = nb >> 4;
+    const uint4* src = reinterpret_cast<const uint4*>(buf + lo);
+    for (int d = 1; d < cs; ++d) {
+        V* dbuf = cl.map_shared_rank(buf, (rank + d) % cs);
+        uint4* dst = reinterpret_cast<uint4*>(dbuf + lo);
+        for (int e = threadIdx.x; e < n16; e += kResThreads) dst[e] = src[e];
+        for (int i = lo + (n16 << 4) / (int)sizeof(V) + threadIdx.x; i < hi; i += kResThreads) dbuf[i] = buf[i];
+    }
+}
+
+// Sum over lanes 0..15 of warp 0 (the CTAs' partials, rank order), the
+// same butterfly in every CTA: bit-identical totals cluster-wide.
+HELP_DEVINL double cta_sum(double v) {
+#pragma unroll
+    for (int o = 8; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// First position in a[b, e) (ascending) whose value is >= v.
+HELP_DEVINL int lower_bound_i(const int* a, int b, int e, int v) {
+    while (b < e) {
+        const int mid = b + ((e - b) >> 1);
+        if (ld_ro(a + mid) < v) b = mid + 1;
+        else e = mid;
+    }
+    return b;
+}
+
+template <class V>
+__global__ void __launch_bounds__(kResThreads, 1) k_cg_resident(const CgArgs<V> A, const ResLayout L, int iters) {
+    cg::cluster_group cl = cg::this_cluster();
+    extern __shared__ __align__(16) unsigned char sm[];
+    __shared__ double red[kResThreads];
+    __shared__ int s_plo, s_phi;
+    __shared__ double s_sc[5];  // rr, rz, beta, p.q, alpha formed by warp 0
+    double* a = reinterpret_cast<double*>(sm + L.a);
+    double* w = reinterpret_cast<double*>(sm + L.w);
+    double* kpart = reinterpret_cast<double*>(sm + L.kpart);  // [cs][k] C^T z_N partials
+    double* s_rz = reinterpret_cast<double*>(sm + L.s_rz);    // [cs] partials
+    double* s_rr = reinterpret_cast<double*>(sm + L.s_rr);
+    double* s_pq = reinterpret_cast<double*>(sm + L.s_pq);
+    double* Wm = reinterpret_cast<double*>(sm + L.W);  // k x k, symmetric
+    V* pf = reinterpret_cast<V*>(sm + L.pf);
+    V* tf = reinterpret_cast<V*>(sm + L.tf);
+    V* xl = reinterpret_cast<V*>(sm + L.xl);
+    V* rl = reinterpret_cast<V*>(sm + L.rl);
+    V* zl = reinterpret_cast<V*>(sm + L.zl);
+    V* ql = reinterpret_cast<V*>(sm + L.ql);
+    V* dl = reinterpret_cast<V*>(sm + L.dl);  // D_S^-1 on own rows
+    V* rP = reinterpret_cast<V*>(sm + L.rp);
+    V* qP = reinterpret_cast<V*>(sm + L.qp);
+    int* pvl = reinterpret_cast<int*>(sm + L.pvl);  // pivot position of own rows (-1: not a pivot)
+    int* pv = reinterpret_cast<int*>(sm + L.piv);   // pivot rows, ascending
+    int* ctp = reinterpret_cast<int*>(sm + L.ct_p); // own entries of C^T: row l in [ctp[l], ctp[l+1])
+    int* cti = reinterpret_cast<int*>(sm + L.ct_i); //   local row index
+    int* ctb = reinterpret_cast<int*>(sm + L.ct_b); // first own entry of C^T row l in HBM
+    V* ctv = reinterpret_cast<V*>(sm + L.ct_v);
+
+    CgScalars* sc = A.sc;
+    if (*(volatile const int*)&sc->done != 0) return;  // same value in every CTA (written before this launch)
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int rank = (int)cl.block_rank(), cs = (int)cl.num_blocks();
+    const int k = A.k;
+    const int lo = min(A.m, rank * L.lr), hi = min(A.m, lo + L.lr);
+    const int clo = min(A.n, rank * L.lc), chi = min(A.n, clo + L.lc);
+    long long it = sc->it;
+    double rz_old = sc->rz_old, rz = sc->rz, rr = sc->rr, alpha = sc->alpha, beta = sc->beta;
+    const double term2 = sc->term2;
+    const long long max_it = sc->max_iter;
+    const bool has_delta = (A.delta != 0.0);
+    const V vd = (V)A.delta;
+
+    // matrix slices and the state of CG iteration `it` into shared memory
+    const LocalCsr<V> Bl = load_rows<V>(A.csr, lo, hi, reinterpret_cast<int*>(sm + L.csr_p),
+                                        reinterpret_cast<int*>(sm + L.csr_i), reinterpret_cast<V*>(sm + L.csr_v));
+    const LocalCsr<V> Bt = load_rows<V>(A.csc, clo, chi, reinterpret_cast<int*>(sm + L.csc_p),
+                                        reinterpret_cast<int*>(sm + L.csc_i), reinterpret_cast<V*>(sm + L.csc_v));
+    const LocalCsr<V> Cl = load_rows<V>(A.c, lo, hi, reinterpret_cast<int*>(sm + L.c_p),
+                                        reinterpret_cast<int*>(sm + L.c_i), reinterpret_cast<V*>(sm + L.c_v));
+    {
+        const V* r = (it & 1) ? A.r1 : A.r0;
+        const V* p = (it & 1) ? A.p1 : A.p0;
+        for (int i = tid; i < A.m; i += kResThreads) pf[i] = p[i];
+        for (int i = lo + tid; i < hi; i += kResThreads) {
+            xl[i - lo] = A.x[i];
+            rl[i - lo] = r[i];
+            dl[i - lo] = ld_ro(A.dsinv + i);
+            pvl[i - lo] = ld_ro(A.pivpos + i);
+        }
+        for (int e = tid; e < k * k; e += kResThreads) Wm[e] = ld_ro(A.W + e);
+        for (int l = tid; l < k; l += kResThreads) {
+            pv[l] = ld_ro(A.piv + l);
+            rP[l] = r[pv[l]];
+            a[l] = A.a[l];
+            // this CTA's entries of row l of C^T (row indices ascending)
+            const int b = ld_ro(A.ct.ptr + l), e = ld_ro(A.ct.ptr + l + 1);
+            const int qb = lower_bound_i(A.ct.idx, b, e, lo);
+            ctb[l] = qb;
+            ctp[l + 1] = lower_bound_i(A.ct.idx, b, e, hi) - qb;
+        }
+        if (tid == 0) {
+            // pivots are in increasing row order: this CTA's pivot rows are l in [plo, phi)
+            s_plo = lower_bound_i(A.piv, 0, k, lo);
+            s_phi = lower_bound_i(A.piv, 0, k, hi);
+        }
+    }
+    __syncthreads();
+    if (tid == 0) {
+        ctp[0] = 0;
+        for (int l = 0; l < k; ++l) ctp[l + 1] += ctp[l];
+    }
+    __syncthreads();
+    for (int l = warp; l < k; l += kResWarps) {
+        const int o = ctp[l], cnt = ctp[l + 1] - o, qb = ctb[l];
+        for (int j = lane; j < cnt; j += 32) {
+            cti[o + j] = ld_ro(A.ct.idx + qb + j) - lo;
+            ctv[o + j] = ld_ro(A.ct.val + qb + j);
+        }
+    }
+    // every CTA has started and loaded its state before any CTA stores into it
+    cl.sync();
+    const int plo = s_plo, phi = s_phi;
+
+    int done = 0;
+    for (int u = 0;; ++u) {
+        // (i) z_N on own rows, r_N.z_N and C^T z_N partials
+        double prz = 0.0;
+        rows_local<V>(
+            Cl, [&](int l) { return (V)a[l]; },
+            [&](int i, V s) {
+                if (pvl[i - lo] < 0) {
+                    const V ri = rl[i - lo];
+                    const V zi = dl[i - lo] * (ri - s);
+                    zl[i - lo] = zi;
+                    prz = fma((double)ri, (double)zi, prz);
+                }
+            });
+        prz = block_sum(prz, red);  // also: zl complete
+        if (tid < cs) *cl.map_shared_rank(s_rz + rank, tid) = prz;
+        // one thread per pivot column l: its entries in this CTA's rows
+        for (int l = tid; l < k; l += kResThreads) {
+            V acc = V(0);
+            for (int q = ctp[l]; q < ctp[l + 1]; ++q) acc = fma_t(ctv[q], zl[cti[q]], acc);
+            for (int c = 0; c < cs; ++c) *cl.map_shared_rank(kpart + (size_t)rank * k + l, c) = (double)acc;
+        }
+        cl.sync();
+        // scalars by warp 0 alone (every FP64 warp instruction costs the SM
+        // the same issue time however few lanes are active): r.r of the
+        // previous step, w = r_P - C^T z_N, rz = r_N.z_N + a.w, beta
+        if (warp == 0) {
+            const double rr_new = cta_sum(lane < cs ? s_rr[lane] : 0.0);
+            double aw = 0.0;
+            for (int l = lane; l < k; l += 32) {
+                double s = 0.0;
+                for (int c = 0; c < cs; ++c) s += kpart[(size_t)c * k + l];
+                const double wl = (double)rP[l] - s;
+                w[l] = wl;
+                aw = fma(a[l], wl, aw);
+            }
+            aw = warp_sum(aw);
+            const double rz_new = cta_sum(lane < cs ? s_rz[lane] : 0.0) + aw;
+            if (lane == 0) {
+                s_sc[0] = rr_new;
+                s_sc[1] = rz_new;
+                s_sc[2] = (it == 0) ? 0.0 : rz_new / rz_old;
+            }
+        }
+        __syncthreads();
+        if (u > 0) {
+            rr = s_sc[0];
+            if (!(rr == rr)) done = 3;
+            else if (rr < term2 || rr == 0.0) done = 1;
+            else if (it >= max_it) done = 2;
+            if (done != 0) break;
+        }
+        if (u == iters) break;
+
+        // (ii) z_P = W w on own pivot rows (W symmetric: column l = row l),
+        // p = z + beta p on own rows
+        rz = s_sc[1];
+        if (!(rz > 0.0)) {
+            done = 3;
+            break;
+        }
+        beta = s_sc[2];
+        for (int l = plo + tid; l < phi; l += kResThreads) {
+            double acc = 0.0;
+            for (int c2 = 0; c2 < k; ++c2) acc = fma(Wm[c2 * k + l], w[c2], acc);
+            zl[pv[l] - lo] = (V)acc;
+        }
+        __syncthreads();
+        {
+            const bool first = (it == 0);
+            const V vb = (V)beta;
+            for (int i = lo + tid; i < hi; i += kResThreads) {
+                const V zi = zl[i - lo];
+                pf[i] = first ? zi : fma_t(vb, pf[i], zi);
+            }
+        }
+        __syncthreads();
+        push_slice(cl, pf, lo, hi, rank, cs);
+        cl.sync();
+
+        // (iii) t = B^T p on own columns
+        rows_local<V>(Bt, [&](int i) { return pf[i]; }, [&](int j, V s) { tf[j] = s; });
+        __syncthreads();
+        push_slice(cl, tf, clo, chi, rank, cs);
+        cl.sync();
+
+        // (iv) q = B t + delta p on own rows, p.q partial, q on own pivot rows
+        double ppq = 0.0;
+        rows_local<V>(
+            Bl, [&](int j) { return tf[j]; },
+            [&](int i, V s) {
+                const V pi = pf[i];
+                const V qi = has_delta ? fma_t(vd, pi, s) : s;
+                ql[i - lo] = qi;
+                ppq = fma((double)pi, (double)qi, ppq);
+            });
+        ppq = block_sum(ppq, red);  // also: ql complete
+        if (tid < cs) *cl.map_shared_rank(s_pq + rank, tid) = ppq;
+        for (int l = plo + tid; l < phi; l += kResThreads) {
+            const V v = ql[pv[l] - lo];
+            for (int c = 0; c < cs; ++c) *cl.map_shared_rank(qP + l, c) = v;
+        }
+        cl.sync();
+        if (warp == 0) {
+            const double pq = cta_sum(lane < cs ? s_pq[lane] : 0.0);
+            if (lane == 0) {
+                s_sc[3] = pq;
+                s_sc[4] = rz / pq;
+            }
+        }
+        __syncthreads();
+        if (!(s_sc[3] > 0.0)) {
+            done = 3;
+            break;
+        }
+        alpha = s_sc[4];
+        rz_old = rz;
+        const V va = (V)alpha;
+        double prr = 0.0;
+        for (int i = lo + tid; i < hi; i += kResThreads) {
+            const V pi = pf[i], qi = ql[i - lo];
+            xl[i - lo] = fma_t(va, pi, xl[i - lo]);
+            const V ri = fma_t(-va, qi, rl[i - lo]);
+            rl[i - lo] = ri;
+            prr = fma((double)ri, (double)ri, prr);
+        }
+        prr = block_sum(prr, red);
+        if (tid < cs) *cl.map_shared_rank(s_rr + rank, tid) = prr;
+        // r_P as the owners computed it (same operands, same rounding), then
+        // a = W r_P, one lane per pivot
+        if (warp == 0) {
+            for (int l = lane; l < k; l += 32) rP[l] = fma_t(-va, qP[l], rP[l]);
+            __syncwarp();
+            for (int l = lane; l < k; l += 32) {
+                double acc = 0.0;
+                for (int c2 = 0; c2 < k; ++c2) acc = fma(Wm[c2 * k + l], (double)rP[c2], acc);
+                a[l] = acc;
+            }
+        }
+        __syncthreads();
+        ++it;
+    }
+    // no CTA leaves while another can still store into its shared memory
+    cl.sync();
+    {
+        V* r = (it & 1) ? A.r1 : A.r0;
+        V* p = (it & 1) ? A.p1 : A.p0;
+        for (int i = lo + tid; i < hi; i += kResThreads) {
+            A.x[i] = xl[i - lo];
+            r[i] = rl[i - lo];
+            p[i] = pf[i];
+        }
+        if (rank == 0) {
+            for (int l = tid; l < k; l += kResThreads) A.a[l] = a[l];
+            if (tid == 0) {
+                sc->it = it;
+                sc->rr = rr;
+                sc->rz = rz;
+                sc->rz_old = rz_old;
+                sc->alpha = alpha;
+                sc->beta = beta;
+                if (done == 3) sc->status = kStatusNumeric;
+                if (done != 0) sc->done = done;
+            }
+        }
+    }
+}
+
+cudaLaunchConfig_t resident_config(int cs, size_t smem, cudaStream_t st, cudaLaunchAttribute* at) {
+    cudaLaunchConfig_t cfg = {};
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = cs;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.gridDim = dim3(cs);
+    cfg.blockDim = dim3(kResThreads);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    return cfg;
+}
+
+}  // namespace
+
+namespace {
+
+// Largest number of nonzeros in one CTA's slice of `per` consecutive rows.
+int64_t slice_max(const int32_t* ptr, int rows, int per) {
+    int64_t mx = 0;
+    for (int lo = 0; lo < rows; lo += per) {
+        const int hi = std::min(rows, lo + per);
+        mx = std::max<int64_t>(mx, (int64_t)ptr[hi] - ptr[lo]);
+    }
+    return mx;
+}
+
+}  // namespace
+
+ResLayout resident_layout(int m, int n, int k, int cs, int vbytes, const int32_t* rp, const int32_t* cp,
+                          const int32_t* crp) {
+    ResLayout L = {};
+    // slices of whole 16-byte words, so DSMEM copies move 16 bytes per store
+    L.lr = (((m + cs - 1) / cs) + 3) & ~3;
+    L.lc = (((n + cs - 1) / cs) + 3) & ~3;
+    const size_t nnz_b = (size_t)slice_max(rp, m, L.lr), nnz_bt = (size_t)slice_max(cp, n, L.lc);
+    const size_t nnz_c = (size_t)slice_max(crp, m, L.lr);
+    size_t o = 0;
+    auto take = [&](size_t bytes) {
+        const size_t at = o;
+        o += (bytes + 15) & ~(size_t)15;
+        return at;
+    };
+    const size_t kk = (size_t)(k > 0 ? k : 1), vb = (size_t)vbytes, lr = (size_t)L.lr, lc = (size_t)L.lc;
+    L.a = take(8 * kk);
+    L.w = take(8 * kk);
+    L.kpart = take(8 * kk * cs);
+    L.s_rz = take(8 * (size_t)cs);
+    L.s_rr = take(8 * (size_t)cs);
+    L.s_pq = take(8 * (size_t)cs);
+    L.W = take(8 * kk * kk);
+    L.pf = take(vb * m);
+    L.tf = take(vb * n);
+    L.xl = take(vb * lr);
+    L.rl = take(vb * lr);
+    L.zl = take(vb * lr);
+    L.ql = take(vb * lr);
+    L.dl = take(vb * lr);
+    L.rp = take(vb * kk);
+    L.qp = take(vb * kk);
+    L.pvl = take(4 * lr);
+    L.piv = take(4 * kk);
+    L.ct_p = take(4 * (kk + 1));
+    L.ct_b = take(4 * kk);
+    L.ct_i = take(4 * std::max<size_t>(nnz_c, 1));
+    L.ct_v = take(vb * std::max<size_t>(nnz_c, 1));
+    L.csr_p = take(4 * (lr + 1));
+    L.csr_i = take(4 * std::max<size_t>(nnz_b, 1));
+    L.csr_v = take(vb * std::max<size_t>(nnz_b, 1));
+    L.csc_p = take(4 * (lc + 1));
+    L.csc_i = take(4 * std::max<size_t>(nnz_bt, 1));
+    L.csc_v = take(vb * std::max<size_t>(nnz_bt, 1));
+    L.c_p = take(4 * (lr + 1));
+    L.c_i = take(4 * std::max<size_t>(nnz_c, 1));
+    L.c_v = take(vb * std::max<size_t>(nnz_c, 1));
+    L.total = o;
+    return L;
+}
+
+// Cluster size (16, else 8) at which k_cg_resident fits the system in shared
+// memory and the GPU can co-schedule the cluster; 0 if none.  rp, cp, crp:
+// host row pointers of B, B^T and C.  *L gets the layout for that size.
+template <class V>
+int cg_resident_configure(int m, int n, int k, const int32_t* rp, const int32_t* cp, const int32_t* crp,
+                          ResLayout* L) {
+    if (k > kResidentMaxPivots) return 0;
+    int dev = 0, optin = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    const size_t static_bytes = sizeof(double) * kResThreads + 64;
+    for (int cs : {16, 8}) {
+        const ResLayout lay = resident_layout(m, n, k, cs, (int)sizeof(V), rp, cp, crp);
+        if (lay.total + static_bytes > (size_t)optin) continue;
+        if (cudaFuncSetAttribute(k_cg_resident<V>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lay.total) !=
+            cudaSuccess) {
+            cudaGetLastError();
+            continue;
+        }
+        if (cs > 8 && cudaFuncSetAttribute(k_cg_resident<V>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) !=
+                          cudaSuccess) {
+            cudaGetLastError();
+            continue;
+        }
+        cudaLaunchAttribute at[1];
+        cudaLaunchConfig_t cfg = resident_config(cs, lay.total, nullptr, at);
+        int nclusters = 0;
+        if (cudaOccupancyMaxActiveClusters(&nclusters, k_cg_resident<V>, &cfg) == cudaSuccess && nclusters >= 1) {
+            *L = lay;
+            return cs;
+        }
+        cudaGetLastError();
+    }
+    return 0;
+}
+
+// Up to `iters` CG iterations in one launch of one cluster of `cs` CTAs.
+template <class V>
+cudaError_t cg_launch_resident(const CgArgs<V>& A, const ResLayout& L, int cs, int iters, cudaStream_t st) {
+    // the shared-memory limit is a property of the function, shared by every
+    // context: set it to this context's size before each launch
+    cudaError_t e = cudaFuncSetAttribute(k_cg_resident<V>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.total);
+    if (e != cudaSuccess) return e;
+    cudaLaunchAttribute at[1];
+    cudaLaunchConfig_t cfg = resident_config(cs, L.total, st, at);
+    return cudaLaunchKernelEx(&cfg, k_cg_resident<V>, A, L, iters);
+}
+
+template int cg_resident_configure<double>(int, int, int, const int32_t*, const int32_t*, const int32_t*,
+                                          ResLayout*);
+template int cg_resident_configure<float>(int, int, int, const int32_t*, const int32_t*, const int32_t*,
+                                         ResLayout*);
+template cudaError_t cg_launch_resident<double>(const CgArgs<double>&, const ResLayout&, int, int, cudaStream_t);
+template cudaError_t cg_launch_resident<float>(const CgArgs<float>&, const ResLayout&, int, int, cudaStream_t);
+
+}  // namespace help

@@ -64,9 +64,13 @@ typedef struct help_pcg_options {
     int32_t warm_start;      /* 1: start CG from the previous solve's x_2 of this renew */
     int32_t fallback;        /* 1: mixed form -- when FP32 refinement stalls or hits its
                                 cap, finish with plain FP64 PCG                          */
-    int32_t cg_path;         /* 0 auto: one thread-block cluster runs whole CG iterations
-                                when the system is small, else the multi-kernel graph;
-                                1 always the graph; 2 always the cluster kernel          */
+    int32_t cg_path;         /* 0 auto: the shared-memory-resident cluster kernel when
+                                the vectors fit one cluster's shared memory (<= 64
+                                pivots, rows of <= 32 G nonzeros), else one thread-block
+                                cluster over L2 when the system is small, else the
+                                multi-kernel graph; 1 always the graph; 2 the cluster
+                                kernel over L2; 3 the resident kernel where it fits
+                                (else as 0)                                              */
 } help_pcg_options;
 
 typedef struct help_pcg_stats {
@@ -86,7 +90,8 @@ typedef struct help_pcg_stats {
     int64_t cg_iterations_fp32;  /* last solve: iterations run in FP32 (mixed)          */
     int32_t cg_launches;         /* last solve                                          */
     int32_t dense_regularised;   /* last renew: pivots raised to the floor in G11       */
-    int32_t cg_path_used;        /* last CG run: 1 multi-kernel graph, 2 single cluster */
+    int32_t cg_path_used;        /* last CG run: 1 multi-kernel graph, 2 single cluster,
+                                    3 single cluster with shared-memory-resident vectors */
     int32_t cluster_ctas;        /* CTAs per cluster of the single-cluster path (0 = unavailable) */
     int32_t learned_warm;        /* last solve: started from the model's warm start     */
     int32_t learned_fallbacks;   /* since construct: model-assisted solves redone plain */

@@ -30,6 +30,16 @@ CASES = {
 }
 
 
+# cases whose vectors fit one cluster's shared memory with rows of <= 32 G
+# nonzeros (the resident CG path); the others fall back to the auto choice
+RESIDENT_CASES = {"random", "mcf"}
+PATH_USED = {
+    "graph": lambda name: {1},
+    "cluster": lambda name: {2},
+    "resident": lambda name: {3} if name in RESIDENT_CASES else {1, 2},
+}
+
+
 @pytest.fixture(scope="module", params=sorted(CASES))
 def case(request):
     lp = CASES[request.param]()
@@ -86,7 +96,7 @@ def test_pivots_diag_schur_precond(case, k):
         assert rel(z, pc.apply(r)) < 1e-8
 
 
-@pytest.mark.parametrize("path", ["graph", "cluster"])
+@pytest.mark.parametrize("path", ["graph", "cluster", "resident"])
 def test_cg_matches_oracle(case, path):
     name, lp, d, rng = case
     rp, ci, v = lp.csr()
@@ -99,13 +109,13 @@ def test_cg_matches_oracle(case, path):
         x, it = g.cg(b)
         st = g.stats()
     assert st["cluster_ctas"] in (8, 16)
-    assert st["cg_path_used"] == {"graph": 1, "cluster": 2}[path]
+    assert st["cg_path_used"] in PATH_USED[path](name)
     xo, ito = ob.pcg(rp, ci, v, d, b, lp.m, lp.n, k, ob.PIVOT_GIVEN, piv, tol=1e-10, max_iter=20000)
     assert rel(x, xo) < 1e-6
     assert abs(it - ito) <= max(3, 0.05 * ito)
 
 
-@pytest.mark.parametrize("path", ["graph", "cluster"])
+@pytest.mark.parametrize("path", ["graph", "cluster", "resident"])
 def test_solve_linear_equation(case, path):
     name, lp, d, rng = case
     b1 = rng.standard_normal(lp.n)
@@ -123,7 +133,7 @@ def test_solve_linear_equation(case, path):
     assert rel(x1, ox1) < 1e-6
 
 
-@pytest.mark.parametrize("path", ["graph", "cluster"])
+@pytest.mark.parametrize("path", ["graph", "cluster", "resident"])
 def test_mixed_precision_solve(case, path):
     name, lp, d, rng = case
     b1 = rng.standard_normal(lp.n)
