@@ -115,24 +115,61 @@ HELP_DEVINL LocalCsr<V> load_rows(const SpmvView<V>& M, int lo, int hi, int* sp,
 
 // Copies buf[lo, hi) of this CTA into the same range of every other CTA's
 // buf.  lo * sizeof(V) and buf are 16-byte aligned (slices start at multiples
-// of 4 elements), so the body moves 16-byte words.
+// of 4 elements), so the body moves 16-byte words.  All (destination, word)
+// pairs in one pass over the whole CTA: a DSMEM store round costs ~250 cycles
+// whatever its width, so a short slice pushed destination by destination
+// would leave most threads idle.
 template <class V>
 HELP_DEVINL void push_slice(cg::cluster_group& cl, V* buf, int lo, int hi, int rank, int cs) {
     if (hi <= lo) return;
-    const int nb = (hi - lo) * (int)sizeof(V);
-    const int n16 = nb >> 4;
+    constexpr int kPer16 = 16 / (int)sizeof(V);
+    const int n16 = (hi - lo) / kPer16;
+    const int per = n16 + (hi - lo - n16 * kPer16);  // 16-byte words, then single elements
+    const int total = (cs - 1) * per;
     const uint4* src = reinterpret_cast<const uint4*>(buf + lo);
-    for (int d = 1; d < cs; ++d) {
-        V* dbuf = cl.map_shared_rank(buf, (rank + d) % cs);
-        uint4* dst = reinterpret_cast<uint4*>(dbuf + lo);
-        for (int e = threadIdx.x; e < n16; e += kResThreads) dst[e] = src[e];
-        for (int i = lo + (n16 << 4) / (int)sizeof(V) + threadIdx.x; i < hi; i += kResThreads) dbuf[i] = buf[i];
+    for (int x = threadIdx.x; x < total; x += kResThreads) {
+        const int d = x / per, e = x - d * per;
+        V* dbuf = cl.map_shared_rank(buf, (rank + 1 + d) % cs);
+        if (e < n16) {
+            reinterpret_cast<uint4*>(dbuf + lo)[e] = src[e];
+        } else {
+            const int i = lo + n16 * kPer16 + (e - n16);
+            dbuf[i] = buf[i];
+        }
     }
 }
 
-// Sum over lanes 0..15 of warp 0 (the CTAs' partials, rank order), the
-// same butterfly in every CTA: bit-identical totals cluster-wide.
-HELP_DEVINL double cta_sum(double v) {
+// Deterministic block-wide sums of two values at once (the tree of
+// block_sum); results valid in every thread.
+HELP_DEVINL void block_sum2(double& u, double& v, double2* red2) {
+    const int tid = threadIdx.x;
+    __syncthreads();
+    red2[tid] = make_double2(u, v);
+    __syncthreads();
+    for (int s = blockDim.x >> 1; s >= 32; s >>= 1) {
+        if (tid < s) {
+            const double2 a = red2[tid], b = red2[tid + s];
+            red2[tid] = make_double2(a.x + b.x, a.y + b.y);
+        }
+        __syncthreads();
+    }
+    if (tid < 32) {
+        double2 w = red2[tid];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            w.x += __shfl_xor_sync(0xffffffffu, w.x, o);
+            w.y += __shfl_xor_sync(0xffffffffu, w.y, o);
+        }
+        if (tid == 0) red2[0] = w;
+    }
+    __syncthreads();
+    u = red2[0].x;
+    v = red2[0].y;
+}
+
+// Sum over the 16 lanes of a half warp (xor butterfly: identical in every
+// lane of the half, and in every CTA for the same inputs).
+HELP_DEVINL double half_sum(double v) {
 #pragma unroll
     for (int o = 8; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
     return v;
@@ -152,11 +189,14 @@ template <class V>
 __global__ void __launch_bounds__(kResThreads, 1) k_cg_resident(const CgArgs<V> A, const ResLayout L, int iters) {
     cg::cluster_group cl = cg::this_cluster();
     extern __shared__ __align__(16) unsigned char sm[];
-    __shared__ double red[kResThreads];
+    __shared__ double2 red2[kResThreads];
+    double* red = reinterpret_cast<double*>(red2);
     __shared__ int s_plo, s_phi;
     __shared__ double s_sc[5];  // rr, rz, beta, p.q, alpha formed by warp 0
+    __shared__ double s_inv_rz;  // 1 / rz of the previous iteration
     double* a = reinterpret_cast<double*>(sm + L.a);
     double* w = reinterpret_cast<double*>(sm + L.w);
+    double* awp = reinterpret_cast<double*>(sm + L.awp);  // a_l w_l
     double* kpart = reinterpret_cast<double*>(sm + L.kpart);  // [cs][k] C^T z_N partials
     double* s_rz = reinterpret_cast<double*>(sm + L.s_rz);    // [cs] partials
     double* s_rr = reinterpret_cast<double*>(sm + L.s_rr);
@@ -221,6 +261,7 @@ __global__ void __launch_bounds__(kResThreads, 1) k_cg_resident(const CgArgs<V> 
             ctp[l + 1] = lower_bound_i(A.ct.idx, b, e, hi) - qb;
         }
         if (tid == 0) {
+            s_inv_rz = (rz_old != 0.0) ? 1.0 / rz_old : 0.0;
             // pivots are in increasing row order: this CTA's pivot rows are l in [plo, phi)
             s_plo = lower_bound_i(A.piv, 0, k, lo);
             s_phi = lower_bound_i(A.piv, 0, k, hi);
@@ -244,8 +285,10 @@ __global__ void __launch_bounds__(kResThreads, 1) k_cg_resident(const CgArgs<V> 
     const int plo = s_plo, phi = s_phi;
 
     int done = 0;
+    double prr = 0.0;  // this CTA's r.r of the last step (iv); reduced with the next r_N.z_N
     for (int u = 0;; ++u) {
-        // (i) z_N on own rows, r_N.z_N and C^T z_N partials
+        // (i) z_N on own rows; r_N.z_N and the previous r.r in one block
+        // reduction; C^T z_N partials
         double prz = 0.0;
         rows_local<V>(
             Cl, [&](int l) { return (V)a[l]; },
@@ -257,8 +300,11 @@ __global__ void __launch_bounds__(kResThreads, 1) k_cg_resident(const CgArgs<V> 
                     prz = fma((double)ri, (double)zi, prz);
                 }
             });
-        prz = block_sum(prz, red);  // also: zl complete
-        if (tid < cs) *cl.map_shared_rank(s_rz + rank, tid) = prz;
+        block_sum2(prz, prr, red2);  // also: zl complete
+        if (tid < cs) {
+            *cl.map_shared_rank(s_rz + rank, tid) = prz;
+            *cl.map_shared_rank(s_rr + rank, tid) = prr;
+        }
         // one thread per pivot column l: its entries in this CTA's rows
         for (int l = tid; l < k; l += kResThreads) {
             V acc = V(0);
@@ -266,25 +312,31 @@ __global__ void __launch_bounds__(kResThreads, 1) k_cg_resident(const CgArgs<V> 
             for (int c = 0; c < cs; ++c) *cl.map_shared_rank(kpart + (size_t)rank * k + l, c) = (double)acc;
         }
         cl.sync();
-        // scalars by warp 0 alone (every FP64 warp instruction costs the SM
-        // the same issue time however few lanes are active): r.r of the
-        // previous step, w = r_P - C^T z_N, rz = r_N.z_N + a.w, beta
-        if (warp == 0) {
-            const double rr_new = cta_sum(lane < cs ? s_rr[lane] : 0.0);
-            double aw = 0.0;
-            for (int l = lane; l < k; l += 32) {
-                double s = 0.0;
-                for (int c = 0; c < cs; ++c) s += kpart[(size_t)c * k + l];
-                const double wl = (double)rP[l] - s;
+        // w = r_P - sum over CTAs of C^T z_N: a half warp per pivot, one lane
+        // per CTA.  (Every FP64 warp instruction holds a sub-partition's FP64
+        // pipe for ~64 cycles however few lanes are active, so the scalar work
+        // is spread over the warps as short trees, not long serial chains.)
+        for (int l0 = 2 * warp; l0 < k; l0 += 2 * kResWarps) {
+            const int l = l0 + (lane >> 4), c = lane & 15;
+            const double v = half_sum((l < k && c < cs) ? kpart[(size_t)c * k + l] : 0.0);
+            if (l < k && c == 0) {
+                const double wl = (double)rP[l] - v;
                 w[l] = wl;
-                aw = fma(a[l], wl, aw);
+                awp[l] = a[l] * wl;
             }
+        }
+        __syncthreads();
+        // r.r of the previous step, rz = r_N.z_N + a.w, beta
+        if (warp == 0) {
+            const double rr_new = half_sum(lane < cs ? s_rr[lane] : 0.0);
+            double aw = 0.0;
+            for (int l = lane; l < k; l += 32) aw += awp[l];
             aw = warp_sum(aw);
-            const double rz_new = cta_sum(lane < cs ? s_rz[lane] : 0.0) + aw;
+            const double rz_new = half_sum(lane < cs ? s_rz[lane] : 0.0) + aw;
             if (lane == 0) {
                 s_sc[0] = rr_new;
                 s_sc[1] = rz_new;
-                s_sc[2] = (it == 0) ? 0.0 : rz_new / rz_old;
+                s_sc[2] = (it == 0) ? 0.0 : rz_new * s_inv_rz;
             }
         }
         __syncthreads();
@@ -297,18 +349,21 @@ __global__ void __launch_bounds__(kResThreads, 1) k_cg_resident(const CgArgs<V> 
         }
         if (u == iters) break;
 
-        // (ii) z_P = W w on own pivot rows (W symmetric: column l = row l),
-        // p = z + beta p on own rows
+        // (ii) z_P = W w on own pivot rows (W symmetric: column l = row l; a
+        // half warp per pivot), p = z + beta p on own rows
         rz = s_sc[1];
         if (!(rz > 0.0)) {
             done = 3;
             break;
         }
         beta = s_sc[2];
-        for (int l = plo + tid; l < phi; l += kResThreads) {
+        for (int l0 = plo + 2 * warp; l0 < phi; l0 += 2 * kResWarps) {
+            const int l = l0 + (lane >> 4), c = lane & 15;
             double acc = 0.0;
-            for (int c2 = 0; c2 < k; ++c2) acc = fma(Wm[c2 * k + l], w[c2], acc);
-            zl[pv[l] - lo] = (V)acc;
+            if (l < phi)
+                for (int c2 = c; c2 < k; c2 += 16) acc = fma(Wm[c2 * k + l], w[c2], acc);
+            acc = half_sum(acc);
+            if (l < phi && c == 0) zl[pv[l] - lo] = (V)acc;
         }
         __syncthreads();
         {
@@ -326,6 +381,8 @@ __global__ void __launch_bounds__(kResThreads, 1) k_cg_resident(const CgArgs<V> 
         // (iii) t = B^T p on own columns
         rows_local<V>(Bt, [&](int i) { return pf[i]; }, [&](int j, V s) { tf[j] = s; });
         __syncthreads();
+        // 1 / rz for the next beta, while the other warps push t
+        if (warp == kResWarps - 1 && lane == 0) s_inv_rz = 1.0 / rz;
         push_slice(cl, tf, clo, chi, rank, cs);
         cl.sync();
 
@@ -347,7 +404,7 @@ __global__ void __launch_bounds__(kResThreads, 1) k_cg_resident(const CgArgs<V> 
         }
         cl.sync();
         if (warp == 0) {
-            const double pq = cta_sum(lane < cs ? s_pq[lane] : 0.0);
+            const double pq = half_sum(lane < cs ? s_pq[lane] : 0.0);
             if (lane == 0) {
                 s_sc[3] = pq;
                 s_sc[4] = rz / pq;
@@ -361,7 +418,7 @@ __global__ void __launch_bounds__(kResThreads, 1) k_cg_resident(const CgArgs<V> 
         alpha = s_sc[4];
         rz_old = rz;
         const V va = (V)alpha;
-        double prr = 0.0;
+        prr = 0.0;
         for (int i = lo + tid; i < hi; i += kResThreads) {
             const V pi = pf[i], qi = ql[i - lo];
             xl[i - lo] = fma_t(va, pi, xl[i - lo]);
@@ -369,18 +426,18 @@ __global__ void __launch_bounds__(kResThreads, 1) k_cg_resident(const CgArgs<V> 
             rl[i - lo] = ri;
             prr = fma((double)ri, (double)ri, prr);
         }
-        prr = block_sum(prr, red);
-        if (tid < cs) *cl.map_shared_rank(s_rr + rank, tid) = prr;
         // r_P as the owners computed it (same operands, same rounding), then
-        // a = W r_P, one lane per pivot
-        if (warp == 0) {
+        // a = W r_P, a half warp per pivot
+        if (warp == 0)
             for (int l = lane; l < k; l += 32) rP[l] = fma_t(-va, qP[l], rP[l]);
-            __syncwarp();
-            for (int l = lane; l < k; l += 32) {
-                double acc = 0.0;
-                for (int c2 = 0; c2 < k; ++c2) acc = fma(Wm[c2 * k + l], (double)rP[c2], acc);
-                a[l] = acc;
-            }
+        __syncthreads();
+        for (int l0 = 2 * warp; l0 < k; l0 += 2 * kResWarps) {
+            const int l = l0 + (lane >> 4), c = lane & 15;
+            double acc = 0.0;
+            if (l < k)
+                for (int c2 = c; c2 < k; c2 += 16) acc = fma(Wm[c2 * k + l], (double)rP[c2], acc);
+            acc = half_sum(acc);
+            if (l < k && c == 0) a[l] = acc;
         }
         __syncthreads();
         ++it;
@@ -459,6 +516,7 @@ ResLayout resident_layout(int m, int n, int k, int cs, int vbytes, const int32_t
     const size_t kk = (size_t)(k > 0 ? k : 1), vb = (size_t)vbytes, lr = (size_t)L.lr, lc = (size_t)L.lc;
     L.a = take(8 * kk);
     L.w = take(8 * kk);
+    L.awp = take(8 * kk);
     L.kpart = take(8 * kk * cs);
     L.s_rz = take(8 * (size_t)cs);
     L.s_rr = take(8 * (size_t)cs);
@@ -505,7 +563,7 @@ int cg_resident_configure(int m, int n, int k, const int32_t* rp, const int32_t*
         cudaGetLastError();
         return 0;
     }
-    const size_t static_bytes = sizeof(double) * kResThreads + 64;
+    const size_t static_bytes = 2 * sizeof(double) * kResThreads + 128;
     for (int cs : {16, 8}) {
         const ResLayout lay = resident_layout(m, n, k, cs, (int)sizeof(V), rp, cp, crp);
         if (lay.total + static_bytes > (size_t)optin) continue;
