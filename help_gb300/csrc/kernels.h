@@ -84,6 +84,7 @@ cudaError_t cg_launch_cluster(const CgArgs<V>& A, int cs, int iters, cudaStream_
 constexpr int kResidentMaxPivots = 64;
 struct ResLayout {
     int lr, lc;
+    int g_b, g_bt, g_c;  // lanes per row of B, B^T, C
     size_t a, w, awp, kpart, s_rz, s_rr, s_pq, W, pf, tf, xl, rl, zl, ql, dl, rp, qp, pvl, piv, ct_p, ct_b, ct_i, ct_v,
         csr_p, csr_i, csr_v, csc_p, csc_i, csc_v, c_p, c_i, c_v, total;
 };

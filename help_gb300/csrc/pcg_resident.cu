@@ -95,7 +95,7 @@ HELP_DEVINL void rows_local(const LocalCsr<V>& M, const XF& xf, const EP& ep) {
 // Copies rows [lo, hi) of a CSR matrix in HBM into shared memory (pointers
 // rebased to 0); returns the slice.
 template <class V>
-HELP_DEVINL LocalCsr<V> load_rows(const SpmvView<V>& M, int lo, int hi, int* sp, int* si, V* sv) {
+HELP_DEVINL LocalCsr<V> load_rows(const SpmvView<V>& M, int lo, int hi, int G, int* sp, int* si, V* sv) {
     const int b = ld_ro(M.ptr + lo);
     for (int r = threadIdx.x; r <= hi - lo; r += kResThreads) sp[r] = ld_ro(M.ptr + lo + r) - b;
     const int e = ld_ro(M.ptr + hi);
@@ -109,7 +109,7 @@ HELP_DEVINL LocalCsr<V> load_rows(const SpmvView<V>& M, int lo, int hi, int* sp,
     L.val = sv;
     L.rows = hi - lo;
     L.row0 = lo;
-    L.G = M.G;
+    L.G = G;
     return L;
 }
 
@@ -203,7 +203,8 @@ __global__ void __launch_bounds__(kResThreads, 1) k_cg_resident(const CgArgs<V> 
     double* s_pq = reinterpret_cast<double*>(sm + L.s_pq);
     double* Wm = reinterpret_cast<double*>(sm + L.W);  // k x k, symmetric
     V* pf = reinterpret_cast<V*>(sm + L.pf);
-    V* tf = reinterpret_cast<V*>(sm + L.tf);
+    constexpr bool kTinL2 = sizeof(V) == 8;           // where t = B^T p is exchanged (see step iii)
+    V* tf = reinterpret_cast<V*>(sm + L.tf);          // FP32: full copy of t
     V* xl = reinterpret_cast<V*>(sm + L.xl);
     V* rl = reinterpret_cast<V*>(sm + L.rl);
     V* zl = reinterpret_cast<V*>(sm + L.zl);
@@ -233,11 +234,11 @@ __global__ void __launch_bounds__(kResThreads, 1) k_cg_resident(const CgArgs<V> 
     const V vd = (V)A.delta;
 
     // matrix slices and the state of CG iteration `it` into shared memory
-    const LocalCsr<V> Bl = load_rows<V>(A.csr, lo, hi, reinterpret_cast<int*>(sm + L.csr_p),
+    const LocalCsr<V> Bl = load_rows<V>(A.csr, lo, hi, L.g_b, reinterpret_cast<int*>(sm + L.csr_p),
                                         reinterpret_cast<int*>(sm + L.csr_i), reinterpret_cast<V*>(sm + L.csr_v));
-    const LocalCsr<V> Bt = load_rows<V>(A.csc, clo, chi, reinterpret_cast<int*>(sm + L.csc_p),
+    const LocalCsr<V> Bt = load_rows<V>(A.csc, clo, chi, L.g_bt, reinterpret_cast<int*>(sm + L.csc_p),
                                         reinterpret_cast<int*>(sm + L.csc_i), reinterpret_cast<V*>(sm + L.csc_v));
-    const LocalCsr<V> Cl = load_rows<V>(A.c, lo, hi, reinterpret_cast<int*>(sm + L.c_p),
+    const LocalCsr<V> Cl = load_rows<V>(A.c, lo, hi, L.g_c, reinterpret_cast<int*>(sm + L.c_p),
                                         reinterpret_cast<int*>(sm + L.c_i), reinterpret_cast<V*>(sm + L.c_v));
     {
         const V* r = (it & 1) ? A.r1 : A.r0;
@@ -378,18 +379,26 @@ __global__ void __launch_bounds__(kResThreads, 1) k_cg_resident(const CgArgs<V> 
         push_slice(cl, pf, lo, hi, rank, cs);
         cl.sync();
 
-        // (iii) t = B^T p on own columns
-        rows_local<V>(Bt, [&](int i) { return pf[i]; }, [&](int j, V s) { tf[j] = s; });
-        __syncthreads();
-        // 1 / rz for the next beta, while the other warps push t
+        // (iii) t = B^T p on own columns.  FP64: to L2, from where every CTA
+        // gathers the t it needs after the barrier -- measured cheaper than
+        // copying all of t (8n bytes) into every CTA's shared memory through
+        // DSMEM (~32 GB/s per SM).  FP32: half the bytes, and the DSMEM copy
+        // wins.
+        if constexpr (kTinL2) {
+            rows_local<V>(Bt, [&](int i) { return pf[i]; }, [&](int j, V s) { A.t[j] = s; });
+        } else {
+            rows_local<V>(Bt, [&](int i) { return pf[i]; }, [&](int j, V s) { tf[j] = s; });
+            __syncthreads();
+        }
+        // 1 / rz for the next beta
         if (warp == kResWarps - 1 && lane == 0) s_inv_rz = 1.0 / rz;
-        push_slice(cl, tf, clo, chi, rank, cs);
+        if constexpr (!kTinL2) push_slice(cl, tf, clo, chi, rank, cs);
         cl.sync();
 
         // (iv) q = B t + delta p on own rows, p.q partial, q on own pivot rows
         double ppq = 0.0;
         rows_local<V>(
-            Bl, [&](int j) { return tf[j]; },
+            Bl, [&](int j) { return kTinL2 ? __ldcg(A.t + j) : tf[j]; },
             [&](int i, V s) {
                 const V pi = pf[i];
                 const V qi = has_delta ? fma_t(vd, pi, s) : s;
@@ -507,6 +516,19 @@ ResLayout resident_layout(int m, int n, int k, int cs, int vbytes, const int32_t
     L.lc = (((n + cs - 1) / cs) + 3) & ~3;
     const size_t nnz_b = (size_t)slice_max(rp, m, L.lr), nnz_bt = (size_t)slice_max(cp, n, L.lc);
     const size_t nnz_c = (size_t)slice_max(crp, m, L.lr);
+    // lanes per row: each FP64 warp instruction costs the same pipe time
+    // however many lanes it uses, so FP64 rows take ~8 nonzeros per lane
+    // (fewer shuffle levels); FP32 rows ~4
+    const int per_lane = vbytes == 8 ? 8 : 4;
+    auto lanes = [&](int64_t nz, int rows) {
+        const double avg = rows > 0 ? (double)nz / rows : 0.0;
+        int g = 1;
+        while (g < 32 && g * per_lane < avg) g *= 2;
+        return g;
+    };
+    L.g_b = lanes(rp[m], m);
+    L.g_bt = lanes(cp[n], n);
+    L.g_c = lanes(crp[m], m);
     size_t o = 0;
     auto take = [&](size_t bytes) {
         const size_t at = o;
@@ -523,7 +545,7 @@ ResLayout resident_layout(int m, int n, int k, int cs, int vbytes, const int32_t
     L.s_pq = take(8 * (size_t)cs);
     L.W = take(8 * kk * kk);
     L.pf = take(vb * m);
-    L.tf = take(vb * n);
+    L.tf = take(vbytes == 8 ? 16 : vb * n);  // t in shared memory for FP32 only
     L.xl = take(vb * lr);
     L.rl = take(vb * lr);
     L.zl = take(vb * lr);
