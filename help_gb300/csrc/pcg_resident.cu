@@ -61,7 +61,7 @@ struct LocalCsr {
 };
 
 // ep(row0 + r, sum) once per row by the group's first lane; G lanes per row.
-template <class V, class XF, class EP>
+template <class V, bool kGatherL2 = false, class XF, class EP>
 HELP_DEVINL void rows_local(const LocalCsr<V>& M, const XF& xf, const EP& ep) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int G = M.G, lg = __ffs(G) - 1;
@@ -75,18 +75,37 @@ HELP_DEVINL void rows_local(const LocalCsr<V>& M, const XF& xf, const EP& ep) {
         }
         V acc = V(0);
         int q = b + sub;
-        for (; q + 3 * G < e; q += 4 * G) {
-            const int c0 = M.idx[q], c1 = M.idx[q + G];
-            const int c2 = M.idx[q + 2 * G], c3 = M.idx[q + 3 * G];
-            const V v0 = M.val[q], v1 = M.val[q + G];
-            const V v2 = M.val[q + 2 * G], v3 = M.val[q + 3 * G];
-            const V x0 = xf(c0), x1 = xf(c1), x2 = xf(c2), x3 = xf(c3);
-            acc = fma_t(v0, x0, acc);
-            acc = fma_t(v1, x1, acc);
-            acc = fma_t(v2, x2, acc);
-            acc = fma_t(v3, x3, acc);
+        if constexpr (kGatherL2) {
+            // gathers from L2: up to 8 entries per lane per round, every load
+            // issued before the first FMA (one L2 round trip for rows of up
+            // to 8 G nonzeros); FMAs in entry order
+            for (; q < e; q += 8 * G) {
+                V xv[8], vv[8];
+#pragma unroll
+                for (int u = 0; u < 8; ++u) {
+                    const int qq = q + u * G;
+                    const bool in = qq < e;
+                    vv[u] = in ? M.val[qq] : V(0);
+                    xv[u] = in ? xf(M.idx[qq]) : V(0);
+                }
+#pragma unroll
+                for (int u = 0; u < 8; ++u)
+                    if (q + u * G < e) acc = fma_t(vv[u], xv[u], acc);
+            }
+        } else {
+            for (; q + 3 * G < e; q += 4 * G) {
+                const int c0 = M.idx[q], c1 = M.idx[q + G];
+                const int c2 = M.idx[q + 2 * G], c3 = M.idx[q + 3 * G];
+                const V v0 = M.val[q], v1 = M.val[q + G];
+                const V v2 = M.val[q + 2 * G], v3 = M.val[q + 3 * G];
+                const V x0 = xf(c0), x1 = xf(c1), x2 = xf(c2), x3 = xf(c3);
+                acc = fma_t(v0, x0, acc);
+                acc = fma_t(v1, x1, acc);
+                acc = fma_t(v2, x2, acc);
+                acc = fma_t(v3, x3, acc);
+            }
+            for (; q < e; q += G) acc = fma_t(M.val[q], xf(M.idx[q]), acc);
         }
-        for (; q < e; q += G) acc = fma_t(M.val[q], xf(M.idx[q]), acc);
         for (int o = G >> 1; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
         if (row < M.rows && sub == 0) ep(M.row0 + row, acc);
     }
@@ -397,7 +416,7 @@ __global__ void __launch_bounds__(kResThreads, 1) k_cg_resident(const CgArgs<V> 
 
         // (iv) q = B t + delta p on own rows, p.q partial, q on own pivot rows
         double ppq = 0.0;
-        rows_local<V>(
+        rows_local<V, kTinL2>(
             Bl, [&](int j) { return kTinL2 ? __ldcg(A.t + j) : tf[j]; },
             [&](int i, V s) {
                 const V pi = pf[i];
