@@ -325,11 +325,14 @@ __global__ void __launch_bounds__(kResThreads, 1) k_cg_resident(const CgArgs<V> 
             *cl.map_shared_rank(s_rz + rank, tid) = prz;
             *cl.map_shared_rank(s_rr + rank, tid) = prr;
         }
-        // one thread per pivot column l: its entries in this CTA's rows
-        for (int l = tid; l < k; l += kResThreads) {
+        // C^T z_N over this CTA's rows, one thread per (pivot l, CTA c): the
+        // cs threads of a pivot form the same sum in the same warp
+        // instructions, and each stores it into one CTA
+        for (int t = tid; t < k * cs; t += kResThreads) {
+            const int l = t / cs, c = t - l * cs;
             V acc = V(0);
             for (int q = ctp[l]; q < ctp[l + 1]; ++q) acc = fma_t(ctv[q], zl[cti[q]], acc);
-            for (int c = 0; c < cs; ++c) *cl.map_shared_rank(kpart + (size_t)rank * k + l, c) = (double)acc;
+            *cl.map_shared_rank(kpart + (size_t)rank * k + l, c) = (double)acc;
         }
         cl.sync();
         // w = r_P - sum over CTAs of C^T z_N: a half warp per pivot, one lane
@@ -346,13 +349,13 @@ __global__ void __launch_bounds__(kResThreads, 1) k_cg_resident(const CgArgs<V> 
             }
         }
         __syncthreads();
-        // r.r of the previous step, rz = r_N.z_N + a.w, beta
+        // r.r of the previous step, rz = r_N.z_N + a.w (the CTAs' r_N.z_N
+        // and the a_l w_l in one warp sum), beta
         if (warp == 0) {
             const double rr_new = half_sum(lane < cs ? s_rr[lane] : 0.0);
-            double aw = 0.0;
-            for (int l = lane; l < k; l += 32) aw += awp[l];
-            aw = warp_sum(aw);
-            const double rz_new = half_sum(lane < cs ? s_rz[lane] : 0.0) + aw;
+            double v = lane < cs ? s_rz[lane] : 0.0;
+            for (int l = lane; l < k; l += 32) v += awp[l];
+            const double rz_new = warp_sum(v);
             if (lane == 0) {
                 s_sc[0] = rr_new;
                 s_sc[1] = rz_new;
@@ -426,9 +429,9 @@ __global__ void __launch_bounds__(kResThreads, 1) k_cg_resident(const CgArgs<V> 
             });
         ppq = block_sum(ppq, red);  // also: ql complete
         if (tid < cs) *cl.map_shared_rank(s_pq + rank, tid) = ppq;
-        for (int l = plo + tid; l < phi; l += kResThreads) {
-            const V v = ql[pv[l] - lo];
-            for (int c = 0; c < cs; ++c) *cl.map_shared_rank(qP + l, c) = v;
+        for (int t = tid; t < (phi - plo) * cs; t += kResThreads) {
+            const int l = plo + t / cs, c = t % cs;
+            *cl.map_shared_rank(qP + l, c) = ql[pv[l] - lo];
         }
         cl.sync();
         if (warp == 0) {
