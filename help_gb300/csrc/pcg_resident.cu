@@ -1,38 +1,40 @@
-// Single-cluster CG with every vector resident in shared memory -- the loop
-// of ConjugateGradient (PCG.cpp:296-395) and the block-form preconditioner
-// of PCG.cpp:183-196 for systems whose vectors fit on one cluster's SMs.
+// Single-cluster CG with the vectors and the matrix resident in shared
+// memory -- the loop of ConjugateGradient (PCG.cpp:296-395) and the
+// block-form preconditioner of PCG.cpp:183-196 for systems that fit on one
+// cluster's SMs.
 //
 // A cluster of 16 (or 8) CTAs, one per SM, owns the solve.  CTA c owns a
 // contiguous slice of the rows of G (m) and of the columns of A (n).  Every
 // CTA keeps in its shared memory
-//   * full copies of p (m) and t = B^T p (n), the two gathered vectors;
+//   * a full copy of p (m), gathered by the B^T product, and in FP32 also a
+//     full copy of t = B^T p (n);
 //   * its own slices of x, r, z, q;
-//   * the pivot-row values r_P, q_P, a = W r_P and w (k each), replicated.
-// and its slices of the matrix (its rows of B, C and D_S^-1, its columns of B
-// -- rows of B^T --, its entries of C^T, and W), copied from HBM once per
-// launch: the acquire side of every cluster barrier invalidates L1, so a
-// matrix read through L1 would come back from L2 after each barrier.  Each
-// iteration is four steps separated by hardware cluster barriers
+//   * the pivot-row values r_P, q_P, a = W r_P and w (k each), replicated;
+//   * its slices of the matrix (its rows of B, C and D_S^-1, its columns of
+//     B -- rows of B^T --, its entries of C^T, and W), copied from HBM once
+//     per launch: the acquire side of every cluster barrier invalidates L1,
+//     so a matrix read through L1 would come back from L2 after each barrier.
+// Each iteration is four steps separated by hardware cluster barriers
 // (barrier.cluster arrive.release / wait.acquire); a CTA hands its results to
 // the others by plain stores into their shared memory (DSMEM) before the
-// barrier, so no CTA ever reads a remote SM and nothing but the launch's
-// first and last copies touches HBM or L2:
-//   (i)   z_N = D_S^-1 (r_N - C a) on own rows; r_N.z_N and the k-vector
-//         C^T z_N over own rows -> every CTA
-//         -- barrier --  stop test on r.r of the previous step (iv)
+// barrier -- except t in FP64, which goes through L2 (see step iii):
+//   (i)   z_N = D_S^-1 (r_N - C a) on own rows; r_N.z_N, the previous step's
+//         r.r and the k-vector C^T z_N over own rows -> every CTA
+//         -- barrier --  stop test on r.r
 //   (ii)  w = r_P - sum C^T z_N, rz = r_N.z_N + a.w, beta, z_P = W w on own
 //         pivot rows, p = z + beta p on own rows -> every CTA's p
 //         -- barrier --
-//   (iii) t = B^T p on own columns -> every CTA's t
+//   (iii) t = B^T p on own columns -> L2 (FP64) / every CTA's t (FP32)
 //         -- barrier --
 //   (iv)  q = B t + delta p on own rows; p.q and q_P -> every CTA
-//         -- barrier --  alpha; x += alpha p, r -= alpha q on own rows, r.r
-//         -> every CTA; r_P -= alpha q_P and a = W r_P in every CTA
-// Every CTA adds the CTAs' partials in rank order, so all of them form
+//         -- barrier --  alpha; x += alpha p, r -= alpha q on own rows;
+//         r_P -= alpha q_P and a = W r_P in every CTA
+// Every CTA adds the CTAs' partials in the same order, so all of them form
 // bit-identical alpha, beta and stopping decisions and leave the loop
-// together.  Row sums use the same lane groups and shuffle order as the
-// whole-GPU kernels (spmv.cuh) for rows of up to 32 G nonzeros, the only
-// rows this path accepts.
+// together.  GB300 issues FP64 at ~2 lanes per clock per SM, and an FP64
+// warp instruction holds its sub-partition's pipe for ~64 cycles however few
+// lanes are active, so the scalar work is written as short trees over many
+// warps rather than serial chains, and rows take several nonzeros per lane.
 #include <cooperative_groups.h>
 
 #include <algorithm>
