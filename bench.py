@@ -181,9 +181,11 @@ def ipm_run(config: int, precision: str, pivots: int | None = None) -> dict:
 
         fns = (native.CONSTRUCT_FN(lambda _c, m, n, cp, ri, v: lib.help_pcg_construct(ctx, m, n, cp, ri, v)),
                native.RENEW_FN(lambda _c, d: lib.help_pcg_renew(ctx, d)), native.SOLVE_FN(solve),
-               native.DESTRUCT_FN(lambda _c: lib.help_pcg_destruct(ctx)))
+               native.DESTRUCT_FN(lambda _c: lib.help_pcg_destruct(ctx)),
+               native.MATVEC_FN(lambda _c, t, s, v, dest: lib.help_pcg_matvec_acc(ctx, t, s, v, dest)))
         f = lambda fn: C.cast(fn, C.c_void_p).value
-        be = native.NeBackend(ctx=None, construct=f(fns[0]), renew=f(fns[1]), solve=f(fns[2]), destruct=f(fns[3]))
+        be = native.NeBackend(ctx=None, construct=f(fns[0]), renew=f(fns[1]), solve=f(fns[2]), destruct=f(fns[3]),
+                              matvec=f(fns[4]))
         t0 = time.perf_counter()
         r = hsd.solve_lp(lp, be)
         wall = time.perf_counter() - t0
@@ -256,6 +258,22 @@ def spmv_large(steps: int, warmup: int, local: int) -> dict:
                          "ms_per_step": round(bt + bb, 4),
                          "passes_gbs": {"BT": round(ab["BT"] / (bt * 1e-3) / 1e9, 1),
                                         "B": round(ab["B"] / (bb * 1e-3) / 1e9, 1)}}
+        # the HSD driver's own products (dest += sign A v, dest += sign A^T y)
+        # on the device copy of A, host buffers in and out (help_pcg_matvec_acc)
+        from help_gb300 import native
+        hp = {}
+        for name, tr, nin, nout in (("A_v", 0, n, m), ("AT_y", 1, m, n)):
+            v = rng.standard_normal(nin)
+            dest = rng.standard_normal(nout)
+            times = []
+            for it in range(4):
+                t0 = time.perf_counter()
+                rc = g.lib.help_pcg_matvec_acc(g.ctx, tr, -1, native.ptr(v), native.ptr(dest))
+                times.append(time.perf_counter() - t0)
+                assert rc == native.HELP_OK
+            hp[name + "_ms"] = round(1e3 * float(np.median(times[1:])), 2)
+        out["hsd_products"] = dict(hp, note="wall time per call through the C ABI with host buffers "
+                                            "(H2D of v and dest, SpMV, D2H), median of 3 after 1 warm-up")
     return out
 
 

@@ -185,8 +185,11 @@ class GpuNormalEquations:
                                                 native.ptr(val), C.byref(nnz)))
         return rp, col[:nnz.value], val[:nnz.value]
 
-    def ne_backend(self) -> native.NeBackend:
-        """Function-pointer table for the native HSD driver (help_hsd_solve)."""
+    def ne_backend(self, gpu_matvec: bool = True) -> native.NeBackend:
+        """Function-pointer table for the native HSD driver (help_hsd_solve).
+        gpu_matvec: the driver's own A x / A^T y products run on this
+        context's device copy of A (help_pcg_matvec_acc); False keeps the
+        driver's host loops (the reference's summation order)."""
         lib = self.lib
         return native.NeBackend(
             ctx=self.ctx.value,
@@ -194,4 +197,5 @@ class GpuNormalEquations:
             renew=C.cast(lib.help_pcg_renew, C.c_void_p).value,
             solve=C.cast(lib.help_pcg_solve, C.c_void_p).value,
             destruct=C.cast(lib.help_pcg_destruct, C.c_void_p).value,
+            matvec=C.cast(lib.help_pcg_matvec_acc, C.c_void_p).value if gpu_matvec else None,
         )

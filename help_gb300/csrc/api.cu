@@ -1043,6 +1043,21 @@ int help_pcg_matvec(help_pcg* ctx, int32_t op, const double* x, double* y) {
     return d2h(ctx, y, ctx->res.as<double>(), nout);
 }
 
+int help_pcg_matvec_acc(help_pcg* ctx, int32_t transpose, int32_t sign, const double* v, double* dest) {
+    if (!ctx || !v || !dest || (sign != 1 && sign != -1)) return HELP_E_ARG;
+    if (!ctx->constructed) return fail(ctx, HELP_E_ARG, "matvec: construct first");
+    CK(cudaSetDevice(ctx->device));
+    const size_t nin = transpose ? ctx->m : ctx->n, nout = transpose ? ctx->n : ctx->m;
+    int rc = h2d(ctx, ctx->xacc.as<double>(), v, nin);
+    if (!rc) rc = h2d(ctx, ctx->res.as<double>(), dest, nout);
+    if (rc) return rc;
+    const SpmvView<double> M = transpose ? view<double>(ctx->pl_csc, ctx->cp, ctx->ri, ctx->avT)
+                                         : view<double>(ctx->pl_csr, ctx->rp, ctx->ci, ctx->av);
+    CK(spmv_launch<double>(kEpiAcc, M, ctx->xacc.as<double>(), ctx->x2.as<double>(), ctx->res.as<double>(), nullptr,
+                           nullptr, (double)sign, spmv_blocks(ctx), kSpmvThreads, ctx->stream));
+    return d2h(ctx, dest, ctx->x2.as<double>(), nout);
+}
+
 int help_pcg_precond_apply(help_pcg* ctx, const double* r, double* z) {
     if (!ctx || !r || !z) return HELP_E_ARG;
     if (!ctx->renewed) return fail(ctx, HELP_E_ARG, "precond: renew first");

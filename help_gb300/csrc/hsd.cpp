@@ -77,8 +77,15 @@ struct Hsd {
     int solves = 0, renews = 0;
     int be_error = 0;
 
-    // Helper.cpp:110-152 over the column lists (CSC keeps the same order)
-    void ATimes(int transpose, int sign, const double* v, double* dest) const {
+    // Helper.cpp:110-152 over the column lists (CSC keeps the same order),
+    // or the backend's device copy of A when it offers one
+    void ATimes(int transpose, int sign, const double* v, double* dest) {
+        if (be->matvec) {
+            const double t = now_s();
+            if (be->matvec(be->ctx, transpose, sign, v, dest) != 0) be_error = 1;
+            backend_s += now_s() - t;
+            return;
+        }
         const int32_t* cp = lp->col_ptr;
         const int32_t* ri = lp->row_ind;
         const double* av = lp->val;

@@ -102,7 +102,8 @@ enum SpmvEpi {
     kEpiRhs = 1,       // y[row] = s - aux[row]                (A D^-1 b1 - b2)
     kEpiBacksub = 2,   // y[row] = s2[row] * (aux[row] - s)    (D^-1 (b1 - A^T x2))
     kEpiResid = 3,     // y[row] = aux[row] - (s + delta * aux2[row])  (rhs - G x)
-    kEpiAddDelta = 4   // y[row] = s + delta * aux[row]
+    kEpiAddDelta = 4,  // y[row] = s + delta * aux[row]
+    kEpiAcc = 5        // y[row] = aux[row] + delta * s        (delta = +-1: the HSD driver's A x / A^T y updates)
 };
 template <class V>
 cudaError_t spmv_launch(int epi, const SpmvView<V>& M, const V* x, V* y, const V* aux, const V* aux2,

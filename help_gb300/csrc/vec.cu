@@ -26,6 +26,8 @@ __global__ void __launch_bounds__(256) k_spmv(const SpmvView<V> M, const V* __re
                 y[row] = (V)(s2[row] * ((double)aux[row] - (double)s));
             } else if (EPI == kEpiResid) {
                 y[row] = aux[row] - fma_t((V)delta, aux2[row], s);
+            } else if (EPI == kEpiAcc) {
+                y[row] = fma_t((V)delta, s, aux[row]);
             } else {
                 y[row] = fma_t((V)delta, aux[row], s);
             }
@@ -118,6 +120,7 @@ cudaError_t spmv_launch(int epi, const SpmvView<V>& M, const V* x, V* y, const V
         case kEpiResid: return spmv_launch_one<V, kEpiResid>(M, x, y, aux, aux2, s2, delta, blocks, threads, stream);
         case kEpiAddDelta:
             return spmv_launch_one<V, kEpiAddDelta>(M, x, y, aux, aux2, s2, delta, blocks, threads, stream);
+        case kEpiAcc: return spmv_launch_one<V, kEpiAcc>(M, x, y, aux, aux2, s2, delta, blocks, threads, stream);
         default:
             return cudaErrorInvalidValue;
     }

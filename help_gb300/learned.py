@@ -183,8 +183,12 @@ class _Recorder:
         def destruct(_c):
             return lib.help_pcg_destruct(ctx)
 
+        @guarded
+        def matvec(_c, t, s, v, dest):
+            return lib.help_pcg_matvec_acc(ctx, t, s, v, dest)
+
         self._fns = (native.CONSTRUCT_FN(construct), native.RENEW_FN(renew), native.SOLVE_FN(solve),
-                     native.DESTRUCT_FN(destruct))
+                     native.DESTRUCT_FN(destruct), native.MATVEC_FN(matvec))
 
     def _snapshot(self, d_ptr) -> None:
         ne = self.ne
@@ -201,7 +205,7 @@ class _Recorder:
     def backend(self) -> native.NeBackend:
         f = lambda fn: C.cast(fn, C.c_void_p).value
         return native.NeBackend(ctx=None, construct=f(self._fns[0]), renew=f(self._fns[1]), solve=f(self._fns[2]),
-                                destruct=f(self._fns[3]))
+                                destruct=f(self._fns[3]), matvec=f(self._fns[4]))
 
 
 def collect(lp, pivots: int, cg_tol: float = 1e-10, device: int = 0) -> list[dict]:

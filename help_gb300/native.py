@@ -126,6 +126,7 @@ CONSTRUCT_FN = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_int32, C.c_int32, C.c_void_p
 RENEW_FN = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_void_p)
 SOLVE_FN = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p)
 DESTRUCT_FN = C.CFUNCTYPE(C.c_int, C.c_void_p)
+MATVEC_FN = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p)
 ONITER_FN = C.CFUNCTYPE(None, C.c_void_p, C.c_int32, C.POINTER(C.c_double))
 
 
@@ -136,6 +137,7 @@ class NeBackend(C.Structure):
         ("renew", C.c_void_p),
         ("solve", C.c_void_p),
         ("destruct", C.c_void_p),
+        ("matvec", C.c_void_p),  # optional: dest += sign * A v / A^T v (NULL: the driver's host loops)
     ]
 
 
@@ -175,7 +177,7 @@ _lp = None
 GPU_SYMBOLS = [
     "help_pcg_default_options", "help_pcg_create", "help_pcg_free", "help_pcg_construct",
     "help_pcg_renew", "help_pcg_solve", "help_pcg_destruct", "help_pcg_get_stats",
-    "help_pcg_last_error", "help_pcg_matvec", "help_pcg_matvec_dev", "help_pcg_precond_apply",
+    "help_pcg_last_error", "help_pcg_matvec", "help_pcg_matvec_dev", "help_pcg_matvec_acc", "help_pcg_precond_apply",
     "help_pcg_get_pivots", "help_pcg_cg", "help_pcg_cg_f32", "help_adat_assemble", "help_adat_matvec_noalloc",
     "help_mlp_create", "help_mlp_free", "help_mlp_last_error", "help_mlp_set_params", "help_mlp_get_params",
     "help_mlp_forward", "help_mlp_loss_grad", "help_mlp_train_step", "help_pcg_attach_mlp", "help_pcg_features",
@@ -217,6 +219,7 @@ def gpu_lib() -> C.CDLL:
         lib.help_pcg_last_error.restype = C.c_char_p
         lib.help_pcg_matvec.argtypes = [vp, i32, dp, dp]
         lib.help_pcg_matvec_dev.argtypes = [vp, i32, i32, vp, vp, vp]
+        lib.help_pcg_matvec_acc.argtypes = [vp, i32, i32, dp, dp]
         lib.help_pcg_precond_apply.argtypes = [vp, dp, dp]
         lib.help_pcg_get_pivots.argtypes = [vp, dp, dp, dp]
         lib.help_pcg_cg.argtypes = [vp, dp, dp, C.POINTER(C.c_int64)]

@@ -145,6 +145,14 @@ int help_pcg_matvec(help_pcg* ctx, int32_t op, const double* x, double* y);
  * fp32 != 0 runs the FP32 copy of B (x, y are then float*). */
 int help_pcg_matvec_dev(help_pcg* ctx, int32_t op, int32_t fp32, const void* x, void* y,
                         void* stream);
+/* dest += sign * A v (transpose 0: v has n entries, dest m) or
+ * dest += sign * A^T v (transpose 1: v has m entries, dest n), sign = +1 or
+ * -1, host arrays, with the device copy of A -- the HSD iteration's own
+ * products (ATimes, Helper.cpp:110-152, called at HSDSolver.cpp:97, :108
+ * and from the direction computation), offered to the driver as the
+ * optional matvec of its backend table.  Each row's products are summed on
+ * the device and added to dest once. */
+int help_pcg_matvec_acc(help_pcg* ctx, int32_t transpose, int32_t sign, const double* v, double* dest);
 /* z = M^-1 r with the last renew's partial-Cholesky preconditioner
  * (Preconditioner, PCG.cpp:183-196), vectors in the original row order. */
 int help_pcg_precond_apply(help_pcg* ctx, const double* r, double* z);

@@ -94,6 +94,11 @@ typedef struct help_ne_backend {
     int (*solve)(void* ctx, const double* d, const double* b_1, const double* b_2,
                  double* x_1, double* x_2);
     int (*destruct)(void* ctx);
+    /* Optional (may be NULL): dest += sign * A v (transpose 0) or
+     * dest += sign * A^T v (transpose 1) with the backend's copy of A -- the
+     * driver's own products (ATimes, Helper.cpp:110-152) done where A
+     * already lives.  NULL: the driver's host loops (the reference's order). */
+    int (*matvec)(void* ctx, int32_t transpose, int32_t sign, const double* v, double* dest);
 } help_ne_backend;
 
 typedef struct help_hsd_options {

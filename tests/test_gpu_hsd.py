@@ -1,0 +1,56 @@
+"""The HSD driver's own products on the device (help_pcg_matvec_acc, the
+optional matvec of the backend table) against numpy and against the driver's
+host loops.
+
+Tolerances: dest += sign * A v to 1e-13 relative (row sums in a different
+order); IPM runs with device and host products reach the same status and
+iteration count and objectives within 1e-9 relative (the products differ in
+rounding only).
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from help_gb300 import backend, hsd, native, lp as L
+
+pytestmark = pytest.mark.gpu
+
+
+def rel(a, b):
+    return np.linalg.norm(np.asarray(a) - np.asarray(b)) / max(np.linalg.norm(b), 1e-300)
+
+
+@pytest.mark.parametrize("transpose", [0, 1])
+@pytest.mark.parametrize("sign", [1, -1])
+def test_matvec_acc(transpose, sign):
+    lp = L.generate(L.spec_zipf(800, 3000, 6, 1.3, 40), 2)  # ragged rows
+    A = np.zeros((lp.m, lp.n))
+    for j in range(lp.n):
+        A[lp.row_ind[lp.col_ptr[j]:lp.col_ptr[j + 1]], j] = lp.val[lp.col_ptr[j]:lp.col_ptr[j + 1]]
+    rng = np.random.default_rng(transpose * 2 + (sign > 0))
+    v = rng.standard_normal(lp.m if transpose else lp.n)
+    dest = rng.standard_normal(lp.n if transpose else lp.m)
+    want = dest + sign * ((A.T if transpose else A) @ v)
+    with backend.GpuNormalEquations(pivots=4) as g:
+        g.LinearEquation_Construct(lp)
+        out = dest.copy()
+        rc = g.lib.help_pcg_matvec_acc(g.ctx, transpose, sign, native.ptr(v), native.ptr(out))
+        assert rc == native.HELP_OK
+        assert rel(out, want) < 1e-13
+        assert g.lib.help_pcg_matvec_acc(g.ctx, transpose, 2, native.ptr(v), native.ptr(out)) != native.HELP_OK
+
+
+@pytest.mark.parametrize("name,spec,seed", [("random", L.spec_random(300, 900, 5), 1),
+                                            ("mcf", L.spec_mcf(8, 3, 2), 4)])
+def test_ipm_device_products_match_host_loops(name, spec, seed):
+    lp = L.generate(spec, seed)
+    runs = {}
+    for dev in (True, False):
+        with backend.GpuNormalEquations(pivots=10, cg_tol=1e-12, cg_max_iter=200000) as g:
+            runs[dev] = hsd.solve_lp(lp, g.ne_backend(gpu_matvec=dev))
+    a, b = runs[True], runs[False]
+    assert a["status"] == b["status"] == 0
+    assert a["iterations"] == b["iterations"]
+    assert abs(a["primal_obj"] - b["primal_obj"]) <= 1e-9 * (1 + abs(b["primal_obj"]))
+    assert a["rel_gap"] < 1e-8 and a["primal_infeas"] < 1e-7

@@ -130,3 +130,34 @@ def test_hsd_driver_objective_matches_scipy():
     r = scipy_opt.linprog(lp.c, A_eq=A, b_eq=lp.b, bounds=(0, None), method="highs")
     assert res["status"] == 0
     assert abs(res["primal_obj"] - r.fun) / (1 + abs(r.fun)) < 1e-8
+
+
+def test_hsd_driver_uses_backend_matvec():
+    """The optional matvec of the backend table replaces the driver's host
+    products: a numpy matvec (dest += sign A v / A^T v) is called for every
+    product and the run matches the host loops to rounding."""
+    import ctypes as C
+    import scipy.sparse as sp
+    from help_gb300 import native
+    lp = L.generate(L.spec_random(80, 240, 5), 3)
+    A = sp.csc_matrix((lp.val, lp.row_ind, lp.col_ptr), shape=(lp.m, lp.n))
+    calls = []
+
+    def matvec(_c, transpose, sign, v, dest):
+        nin, nout = (lp.m, lp.n) if transpose else (lp.n, lp.m)
+        vv = np.ctypeslib.as_array(C.cast(v, C.POINTER(C.c_double)), (nin,))
+        dd = np.ctypeslib.as_array(C.cast(dest, C.POINTER(C.c_double)), (nout,))
+        dd += sign * ((A.T if transpose else A) @ vv)
+        calls.append(transpose)
+        return 0
+
+    fn = native.MATVEC_FN(matvec)
+    ora = ob.OracleNormalEquations(pivots=10, tol=1e-14, max_iter=10**6)
+    be = ora.ne_backend()
+    be.matvec = C.cast(fn, C.c_void_p).value
+    res = hsd.solve_lp(lp, be)
+    ora2 = ob.OracleNormalEquations(pivots=10, tol=1e-14, max_iter=10**6)
+    ref = hsd.solve_lp(lp, ora2.ne_backend())
+    assert res["status"] == ref["status"] == 0
+    assert calls.count(0) > 0 and calls.count(1) > 0
+    assert abs(res["primal_obj"] - ref["primal_obj"]) <= 1e-9 * (1 + abs(ref["primal_obj"]))
