@@ -131,6 +131,23 @@ def fixed_warm_params() -> np.ndarray:
     return p
 
 
+def diag_head_only(params: np.ndarray) -> np.ndarray:
+    """The trained network's Schur-diagonal correction with the warm-start
+    head replaced by the constant 1 (the warm start without the network)."""
+    p = np.array(params, np.float32, copy=True)
+    p[native.MLP_OFF_W3 + native.MLP_HIDDEN:native.MLP_OFF_W3 + 2 * native.MLP_HIDDEN] = 0.0  # W3 is [out][hidden]
+    p[native.MLP_OFF_B3 + 1] = 1.0
+    return p
+
+
+def warm_head_only(params: np.ndarray) -> np.ndarray:
+    """The trained network's warm-start scales with no diagonal correction."""
+    p = np.array(params, np.float32, copy=True)
+    p[native.MLP_OFF_W3:native.MLP_OFF_W3 + native.MLP_HIDDEN] = 0.0
+    p[native.MLP_OFF_B3] = 0.0
+    return p
+
+
 def zero_params() -> np.ndarray:
     """A model whose outputs are 0: no correction, no warm start (alpha = 0)."""
     p = np.zeros(native.MLP_PARAMS, np.float32)
