@@ -191,7 +191,7 @@ class GpuNormalEquations:
         context's device copy of A (help_pcg_matvec_acc); False keeps the
         driver's host loops (the reference's summation order)."""
         lib = self.lib
-        return native.NeBackend(
+        be = native.NeBackend(
             ctx=self.ctx.value,
             construct=C.cast(lib.help_pcg_construct, C.c_void_p).value,
             renew=C.cast(lib.help_pcg_renew, C.c_void_p).value,
@@ -199,3 +199,5 @@ class GpuNormalEquations:
             destruct=C.cast(lib.help_pcg_destruct, C.c_void_p).value,
             matvec=C.cast(lib.help_pcg_matvec_acc, C.c_void_p).value if gpu_matvec else None,
         )
+        be._owner = self  # the table holds self.ctx: keep the context alive as long as the table
+        return be

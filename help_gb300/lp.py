@@ -67,6 +67,13 @@ class LP:
         if rc != 0:
             raise RuntimeError("help_lp_write_mps failed (%d)" % rc)
 
+    def write_bin(self, path: str) -> None:
+        """Binary fast path (help_lp_write_bin): the CSC arrays, b, c, row types."""
+        lib = native.lp_lib()
+        rc = lib.help_lp_write_bin(C.byref(self.as_struct()), path.encode())
+        if rc != 0:
+            raise OSError("help_lp_write_bin failed (%d): %s" % (rc, lib.help_lp_last_error().decode()))
+
 
 def spec_random(m: int, n: int, k: int) -> native.LpSpec:
     return native.LpSpec(kind=native.HELP_LP_RANDOM, m=m, n=n, nnz_per_col=k)
@@ -97,12 +104,7 @@ CONFIGS = {
 }
 
 
-def generate(spec: native.LpSpec, seed: int = 0, name: str = "") -> LP:
-    lib = native.lp_lib()
-    s = native.LpStruct()
-    rc = lib.help_lp_generate(C.byref(spec), C.c_uint64(seed), C.byref(s))
-    if rc != 0:
-        raise ValueError("help_lp_generate failed (%d)" % rc)
+def _from_struct(lib, s, name: str) -> LP:
     try:
         n, nnz, m = s.n, s.nnz, s.m
         lp = LP(
@@ -118,6 +120,36 @@ def generate(spec: native.LpSpec, seed: int = 0, name: str = "") -> LP:
     finally:
         lib.help_lp_free(C.byref(s))
     return lp
+
+
+def generate(spec: native.LpSpec, seed: int = 0, name: str = "") -> LP:
+    lib = native.lp_lib()
+    s = native.LpStruct()
+    rc = lib.help_lp_generate(C.byref(spec), C.c_uint64(seed), C.byref(s))
+    if rc != 0:
+        raise ValueError("help_lp_generate failed (%d)" % rc)
+    return _from_struct(lib, s, name)
+
+
+def read_mps(path: str) -> LP:
+    """An MPS file in the standard form the HSD driver takes (help_lp_read_mps:
+    E/L/G rows, slacks appended for L/G rows, x >= 0 only)."""
+    lib = native.lp_lib()
+    s = native.LpStruct()
+    rc = lib.help_lp_read_mps(path.encode(), C.byref(s))
+    if rc != 0:
+        raise ValueError("help_lp_read_mps failed (%d): %s" % (rc, lib.help_lp_last_error().decode()))
+    return _from_struct(lib, s, path)
+
+
+def read_bin(path: str) -> LP:
+    """An instance written by LP.write_bin / help_lp_write_bin."""
+    lib = native.lp_lib()
+    s = native.LpStruct()
+    rc = lib.help_lp_read_bin(path.encode(), C.byref(s))
+    if rc != 0:
+        raise ValueError("help_lp_read_bin failed (%d): %s" % (rc, lib.help_lp_last_error().decode()))
+    return _from_struct(lib, s, path)
 
 
 def make_lp(config: int, seed: int = 0) -> LP:

@@ -183,7 +183,8 @@ GPU_SYMBOLS = [
     "help_mlp_forward", "help_mlp_loss_grad", "help_mlp_train_step", "help_pcg_attach_mlp", "help_pcg_features",
 ]
 LP_SYMBOLS = [
-    "help_lp_generate", "help_lp_free", "help_lp_write_mps", "help_csc_to_csr",
+    "help_lp_generate", "help_lp_free", "help_lp_write_mps", "help_csc_to_csr", "help_lp_read_mps",
+    "help_lp_write_bin", "help_lp_read_bin", "help_lp_last_error",
     "help_hsd_default_options", "help_hsd_solve",
 ]
 
@@ -251,6 +252,11 @@ def lp_lib() -> C.CDLL:
         lib.help_lp_free.argtypes = [C.POINTER(LpStruct)]
         lib.help_lp_free.restype = None
         lib.help_lp_write_mps.argtypes = [C.POINTER(LpStruct), C.c_char_p]
+        lib.help_lp_read_mps.argtypes = [C.c_char_p, C.POINTER(LpStruct)]
+        lib.help_lp_write_bin.argtypes = [C.POINTER(LpStruct), C.c_char_p]
+        lib.help_lp_read_bin.argtypes = [C.c_char_p, C.POINTER(LpStruct)]
+        lib.help_lp_last_error.argtypes = []
+        lib.help_lp_last_error.restype = C.c_char_p
         lib.help_csc_to_csr.argtypes = [C.c_int32, C.c_int32] + [C.c_void_p] * 6
         lib.help_hsd_default_options.argtypes = [C.POINTER(HsdOptions)]
         lib.help_hsd_default_options.restype = None

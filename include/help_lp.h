@@ -66,6 +66,29 @@ void help_lp_free(help_lp* lp);
  * card positions 4/14/24).  Returns 0 on success. */
 int help_lp_write_mps(const help_lp* lp, const char* path);
 
+/* Reads an MPS file (fixed or free layout: fields separated by blanks, names
+ * without blanks) into the standard form above, as the reference's MPSRead
+ * (MPSRead.cpp:76-219) and row standardisation (Crushing.cpp:71-99) do for
+ * the problems the HSD driver takes: rows N (the first is the objective,
+ * minimised), E, L, G; L and G rows get a slack column (+1 / -1) appended
+ * after the structural columns in row order; entries of unknown rows and
+ * entries below 1e-8 in magnitude are dropped (MPSRead.cpp:148-163); rows are
+ * sorted inside each column and a repeated (row, column) entry is an error.
+ * RANGES and every bound other than x >= 0 (LO 0, PL) are rejected, as are
+ * integer markers.  Returns 0, -1 bad arguments, -2 I/O error, -3 format
+ * error (help_lp_last_error() tells which line and why). */
+int help_lp_read_mps(const char* path, help_lp* out);
+
+/* Binary fast path for large instances (no text parsing): a 64-byte header
+ * ("HELPLP01", m, n, n_struct, nnz as int64) followed by col_ptr (int32,
+ * n+1), row_ind (int32, nnz), val (f64, nnz), b (f64, m), c (f64, n),
+ * row_type (m bytes), little-endian.  Return codes as help_lp_read_mps. */
+int help_lp_write_bin(const help_lp* lp, const char* path);
+int help_lp_read_bin(const char* path, help_lp* out);
+
+/* Message of the last failed read on this thread ("" if none). */
+const char* help_lp_last_error(void);
+
 /* Row-major copy (CSR, column indices sorted inside each row) of a CSC matrix. */
 int help_csc_to_csr(int32_t m, int32_t n, const int32_t* col_ptr, const int32_t* row_ind,
                     const double* val, int32_t* row_ptr, int32_t* col_ind, double* val_out);

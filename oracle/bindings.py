@@ -218,10 +218,12 @@ class OracleNormalEquations:
     def ne_backend(self):
         from help_gb300 import native
         L = self.L
-        return native.NeBackend(ctx=self.ctx, construct=C.cast(L.oracle_ne_construct, C.c_void_p).value,
-                                renew=C.cast(L.oracle_ne_renew, C.c_void_p).value,
-                                solve=C.cast(L.oracle_ne_solve, C.c_void_p).value,
-                                destruct=C.cast(L.oracle_ne_destruct, C.c_void_p).value)
+        be = native.NeBackend(ctx=self.ctx, construct=C.cast(L.oracle_ne_construct, C.c_void_p).value,
+                              renew=C.cast(L.oracle_ne_renew, C.c_void_p).value,
+                              solve=C.cast(L.oracle_ne_solve, C.c_void_p).value,
+                              destruct=C.cast(L.oracle_ne_destruct, C.c_void_p).value)
+        be._owner = self  # the table holds self.ctx: keep the context alive as long as the table
+        return be
 
     def __del__(self):
         try:
