@@ -82,14 +82,22 @@ cudaError_t cg_launch_cluster(const CgArgs<V>& A, int cs, int iters, cudaStream_
 // rows of B and B^T all hold <= 32 G nonzeros.  Byte offsets into the
 // kernel's dynamic shared memory; lr / lc rows / columns per CTA.
 constexpr int kResidentMaxPivots = 64;
+// matrix slices read from L2 every iteration (when they do not fit shared
+// memory) up to this much work per iteration, 2 (nnz(A) + nnz(C)): beyond
+// it the whole-GPU graph's 152 SMs win over one cluster's 16 (measured FP64
+// us per CG iteration, resident / graph: 29 / 43 at 120k nonzeros, 36 / 38
+// at 117k (MCF), 42 / 43 at 150k with k = 64, 64 / 46 at 300k)
+constexpr int64_t kResidentL2Work = 320000;
 struct ResLayout {
     int lr, lc;
+    int mat_smem;        // 1: matrix slices in shared memory, 0: read from L2
+    int t_smem;          // 1: t = B^T p copied into every CTA (FP32), 0: exchanged through L2
     int g_b, g_bt, g_c;  // lanes per row of B, B^T, C
     size_t a, w, awp, kpart, s_rz, s_rr, s_pq, W, pf, tf, xl, rl, zl, ql, dl, rp, qp, pvl, piv, ct_p, ct_b, ct_i, ct_v,
         csr_p, csr_i, csr_v, csc_p, csc_i, csc_v, c_p, c_i, c_v, total;
 };
 ResLayout resident_layout(int m, int n, int k, int cs, int vbytes, const int32_t* rp, const int32_t* cp,
-                          const int32_t* crp);
+                          const int32_t* crp, bool mat_smem, bool t_smem);
 template <class V>
 int cg_resident_configure(int m, int n, int k, const int32_t* rp, const int32_t* cp, const int32_t* crp,
                           ResLayout* L);

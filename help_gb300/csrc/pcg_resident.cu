@@ -113,6 +113,19 @@ HELP_DEVINL void rows_local(const LocalCsr<V>& M, const XF& xf, const EP& ep) {
     }
 }
 
+// Rows [lo, hi) of a CSR matrix in HBM, read in place.
+template <class V>
+HELP_DEVINL LocalCsr<V> global_rows(const SpmvView<V>& M, int lo, int hi, int G) {
+    LocalCsr<V> L;
+    L.ptr = M.ptr + lo;  // absolute offsets into idx / val
+    L.idx = M.idx;
+    L.val = M.val;
+    L.rows = hi - lo;
+    L.row0 = lo;
+    L.G = G;
+    return L;
+}
+
 // Copies rows [lo, hi) of a CSR matrix in HBM into shared memory (pointers
 // rebased to 0); returns the slice.
 template <class V>
@@ -206,7 +219,7 @@ HELP_DEVINL int lower_bound_i(const int* a, int b, int e, int v) {
     return b;
 }
 
-template <class V>
+template <class V, bool kMatSmem, bool kTsmem>
 __global__ void __launch_bounds__(kResThreads, 1) k_cg_resident(const CgArgs<V> A, const ResLayout L, int iters) {
     cg::cluster_group cl = cg::this_cluster();
     extern __shared__ __align__(16) unsigned char sm[];
@@ -224,8 +237,8 @@ __global__ void __launch_bounds__(kResThreads, 1) k_cg_resident(const CgArgs<V> 
     double* s_pq = reinterpret_cast<double*>(sm + L.s_pq);
     double* Wm = reinterpret_cast<double*>(sm + L.W);  // k x k, symmetric
     V* pf = reinterpret_cast<V*>(sm + L.pf);
-    constexpr bool kTinL2 = sizeof(V) == 8;           // where t = B^T p is exchanged (see step iii)
-    V* tf = reinterpret_cast<V*>(sm + L.tf);          // FP32: full copy of t
+    constexpr bool kTinL2 = !kTsmem;                  // where t = B^T p is exchanged (see step iii)
+    V* tf = reinterpret_cast<V*>(sm + L.tf);          // full copy of t when kTsmem
     V* xl = reinterpret_cast<V*>(sm + L.xl);
     V* rl = reinterpret_cast<V*>(sm + L.rl);
     V* zl = reinterpret_cast<V*>(sm + L.zl);
@@ -255,12 +268,21 @@ __global__ void __launch_bounds__(kResThreads, 1) k_cg_resident(const CgArgs<V> 
     const V vd = (V)A.delta;
 
     // matrix slices and the state of CG iteration `it` into shared memory
-    const LocalCsr<V> Bl = load_rows<V>(A.csr, lo, hi, L.g_b, reinterpret_cast<int*>(sm + L.csr_p),
-                                        reinterpret_cast<int*>(sm + L.csr_i), reinterpret_cast<V*>(sm + L.csr_v));
-    const LocalCsr<V> Bt = load_rows<V>(A.csc, clo, chi, L.g_bt, reinterpret_cast<int*>(sm + L.csc_p),
-                                        reinterpret_cast<int*>(sm + L.csc_i), reinterpret_cast<V*>(sm + L.csc_v));
-    const LocalCsr<V> Cl = load_rows<V>(A.c, lo, hi, L.g_c, reinterpret_cast<int*>(sm + L.c_p),
-                                        reinterpret_cast<int*>(sm + L.c_i), reinterpret_cast<V*>(sm + L.c_v));
+    LocalCsr<V> Bl, Bt, Cl;
+    if constexpr (kMatSmem) {
+        Bl = load_rows<V>(A.csr, lo, hi, L.g_b, reinterpret_cast<int*>(sm + L.csr_p),
+                          reinterpret_cast<int*>(sm + L.csr_i), reinterpret_cast<V*>(sm + L.csr_v));
+        Bt = load_rows<V>(A.csc, clo, chi, L.g_bt, reinterpret_cast<int*>(sm + L.csc_p),
+                          reinterpret_cast<int*>(sm + L.csc_i), reinterpret_cast<V*>(sm + L.csc_v));
+        Cl = load_rows<V>(A.c, lo, hi, L.g_c, reinterpret_cast<int*>(sm + L.c_p),
+                          reinterpret_cast<int*>(sm + L.c_i), reinterpret_cast<V*>(sm + L.c_v));
+    } else {
+        // larger systems: the slices stay in HBM / L2 and are read every
+        // iteration (each barrier invalidates L1)
+        Bl = global_rows<V>(A.csr, lo, hi, L.g_b);
+        Bt = global_rows<V>(A.csc, clo, chi, L.g_bt);
+        Cl = global_rows<V>(A.c, lo, hi, L.g_c);
+    }
     {
         const V* r = (it & 1) ? A.r1 : A.r0;
         const V* p = (it & 1) ? A.p1 : A.p0;
@@ -312,7 +334,7 @@ __global__ void __launch_bounds__(kResThreads, 1) k_cg_resident(const CgArgs<V> 
         // (i) z_N on own rows; r_N.z_N and the previous r.r in one block
         // reduction; C^T z_N partials
         double prz = 0.0;
-        rows_local<V>(
+        rows_local<V, !kMatSmem>(
             Cl, [&](int l) { return (V)a[l]; },
             [&](int i, V s) {
                 if (pvl[i - lo] < 0) {
@@ -407,11 +429,11 @@ __global__ void __launch_bounds__(kResThreads, 1) k_cg_resident(const CgArgs<V> 
         // gathers the t it needs after the barrier -- measured cheaper than
         // copying all of t (8n bytes) into every CTA's shared memory through
         // DSMEM (~32 GB/s per SM).  FP32: half the bytes, and the DSMEM copy
-        // wins.
+        // wins where the copy fits in shared memory.
         if constexpr (kTinL2) {
-            rows_local<V>(Bt, [&](int i) { return pf[i]; }, [&](int j, V s) { A.t[j] = s; });
+            rows_local<V, !kMatSmem>(Bt, [&](int i) { return pf[i]; }, [&](int j, V s) { A.t[j] = s; });
         } else {
-            rows_local<V>(Bt, [&](int i) { return pf[i]; }, [&](int j, V s) { tf[j] = s; });
+            rows_local<V, !kMatSmem>(Bt, [&](int i) { return pf[i]; }, [&](int j, V s) { tf[j] = s; });
             __syncthreads();
         }
         // 1 / rz for the next beta
@@ -421,7 +443,7 @@ __global__ void __launch_bounds__(kResThreads, 1) k_cg_resident(const CgArgs<V> 
 
         // (iv) q = B t + delta p on own rows, p.q partial, q on own pivot rows
         double ppq = 0.0;
-        rows_local<V, kTinL2>(
+        rows_local<V, kTinL2 || !kMatSmem>(
             Bl, [&](int j) { return kTinL2 ? __ldcg(A.t + j) : tf[j]; },
             [&](int i, V s) {
                 const V pi = pf[i];
@@ -533,8 +555,10 @@ int64_t slice_max(const int32_t* ptr, int rows, int per) {
 }  // namespace
 
 ResLayout resident_layout(int m, int n, int k, int cs, int vbytes, const int32_t* rp, const int32_t* cp,
-                          const int32_t* crp) {
+                          const int32_t* crp, bool mat_smem, bool t_smem) {
     ResLayout L = {};
+    L.mat_smem = mat_smem ? 1 : 0;
+    L.t_smem = t_smem ? 1 : 0;
     // slices of whole 16-byte words, so DSMEM copies move 16 bytes per store
     L.lr = (((m + cs - 1) / cs) + 3) & ~3;
     L.lc = (((n + cs - 1) / cs) + 3) & ~3;
@@ -569,7 +593,7 @@ ResLayout resident_layout(int m, int n, int k, int cs, int vbytes, const int32_t
     L.s_pq = take(8 * (size_t)cs);
     L.W = take(8 * kk * kk);
     L.pf = take(vb * m);
-    L.tf = take(vbytes == 8 ? 16 : vb * n);  // t in shared memory for FP32 only
+    L.tf = take(t_smem ? vb * n : 16);
     L.xl = take(vb * lr);
     L.rl = take(vb * lr);
     L.zl = take(vb * lr);
@@ -583,22 +607,38 @@ ResLayout resident_layout(int m, int n, int k, int cs, int vbytes, const int32_t
     L.ct_b = take(4 * kk);
     L.ct_i = take(4 * std::max<size_t>(nnz_c, 1));
     L.ct_v = take(vb * std::max<size_t>(nnz_c, 1));
-    L.csr_p = take(4 * (lr + 1));
-    L.csr_i = take(4 * std::max<size_t>(nnz_b, 1));
-    L.csr_v = take(vb * std::max<size_t>(nnz_b, 1));
-    L.csc_p = take(4 * (lc + 1));
-    L.csc_i = take(4 * std::max<size_t>(nnz_bt, 1));
-    L.csc_v = take(vb * std::max<size_t>(nnz_bt, 1));
-    L.c_p = take(4 * (lr + 1));
-    L.c_i = take(4 * std::max<size_t>(nnz_c, 1));
-    L.c_v = take(vb * std::max<size_t>(nnz_c, 1));
+    if (mat_smem) {
+        L.csr_p = take(4 * (lr + 1));
+        L.csr_i = take(4 * std::max<size_t>(nnz_b, 1));
+        L.csr_v = take(vb * std::max<size_t>(nnz_b, 1));
+        L.csc_p = take(4 * (lc + 1));
+        L.csc_i = take(4 * std::max<size_t>(nnz_bt, 1));
+        L.csc_v = take(vb * std::max<size_t>(nnz_bt, 1));
+        L.c_p = take(4 * (lr + 1));
+        L.c_i = take(4 * std::max<size_t>(nnz_c, 1));
+        L.c_v = take(vb * std::max<size_t>(nnz_c, 1));
+    }
     L.total = o;
     return L;
 }
 
+// The kernel for a layout: FP64 always exchanges t through L2 (measured
+// faster), FP32 through shared memory where t fits there.
+template <class V>
+const void* resident_fn(bool mat_smem, bool t_smem) {
+    if constexpr (sizeof(V) == 8) {
+        return mat_smem ? (const void*)k_cg_resident<V, true, false> : (const void*)k_cg_resident<V, false, false>;
+    } else {
+        if (mat_smem) return t_smem ? (const void*)k_cg_resident<V, true, true> : (const void*)k_cg_resident<V, true, false>;
+        return t_smem ? (const void*)k_cg_resident<V, false, true> : (const void*)k_cg_resident<V, false, false>;
+    }
+}
+
 // Cluster size (16, else 8) at which k_cg_resident fits the system in shared
-// memory and the GPU can co-schedule the cluster; 0 if none.  rp, cp, crp:
-// host row pointers of B, B^T and C.  *L gets the layout for that size.
+// memory and the GPU can co-schedule the cluster; 0 if none.  Tries the
+// matrix slices in shared memory first, then (for at most kResidentL2Work
+// per iteration) in L2.  rp, cp, crp: host row pointers of B, B^T and C.
+// *L gets the layout.
 template <class V>
 int cg_resident_configure(int m, int n, int k, const int32_t* rp, const int32_t* cp, const int32_t* crp,
                           ResLayout* L) {
@@ -609,28 +649,33 @@ int cg_resident_configure(int m, int n, int k, const int32_t* rp, const int32_t*
         cudaGetLastError();
         return 0;
     }
+    const int64_t work = 2 * ((int64_t)rp[m] + crp[m]);
     const size_t static_bytes = 2 * sizeof(double) * kResThreads + 128;
-    for (int cs : {16, 8}) {
-        const ResLayout lay = resident_layout(m, n, k, cs, (int)sizeof(V), rp, cp, crp);
-        if (lay.total + static_bytes > (size_t)optin) continue;
-        if (cudaFuncSetAttribute(k_cg_resident<V>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lay.total) !=
-            cudaSuccess) {
+    for (int variant = 0; variant < 4; ++variant) {
+        const bool mat_smem = variant < 2, t_smem = (variant & 1) == 0;
+        if (!mat_smem && work > kResidentL2Work) break;
+        if (t_smem && sizeof(V) == 8) continue;
+        const void* fn = resident_fn<V>(mat_smem, t_smem);
+        for (int cs : {16, 8}) {
+            const ResLayout lay = resident_layout(m, n, k, cs, (int)sizeof(V), rp, cp, crp, mat_smem, t_smem);
+            if (lay.total + static_bytes > (size_t)optin) continue;
+            if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lay.total) != cudaSuccess) {
+                cudaGetLastError();
+                continue;
+            }
+            if (cs > 8 && cudaFuncSetAttribute(fn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess) {
+                cudaGetLastError();
+                continue;
+            }
+            cudaLaunchAttribute at[1];
+            cudaLaunchConfig_t cfg = resident_config(cs, lay.total, nullptr, at);
+            int nclusters = 0;
+            if (cudaOccupancyMaxActiveClusters(&nclusters, fn, &cfg) == cudaSuccess && nclusters >= 1) {
+                *L = lay;
+                return cs;
+            }
             cudaGetLastError();
-            continue;
         }
-        if (cs > 8 && cudaFuncSetAttribute(k_cg_resident<V>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) !=
-                          cudaSuccess) {
-            cudaGetLastError();
-            continue;
-        }
-        cudaLaunchAttribute at[1];
-        cudaLaunchConfig_t cfg = resident_config(cs, lay.total, nullptr, at);
-        int nclusters = 0;
-        if (cudaOccupancyMaxActiveClusters(&nclusters, k_cg_resident<V>, &cfg) == cudaSuccess && nclusters >= 1) {
-            *L = lay;
-            return cs;
-        }
-        cudaGetLastError();
     }
     return 0;
 }
@@ -640,11 +685,13 @@ template <class V>
 cudaError_t cg_launch_resident(const CgArgs<V>& A, const ResLayout& L, int cs, int iters, cudaStream_t st) {
     // the shared-memory limit is a property of the function, shared by every
     // context: set it to this context's size before each launch
-    cudaError_t e = cudaFuncSetAttribute(k_cg_resident<V>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.total);
+    const void* fn = resident_fn<V>(L.mat_smem != 0, L.t_smem != 0);
+    cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.total);
     if (e != cudaSuccess) return e;
     cudaLaunchAttribute at[1];
     cudaLaunchConfig_t cfg = resident_config(cs, L.total, st, at);
-    return cudaLaunchKernelEx(&cfg, k_cg_resident<V>, A, L, iters);
+    void* args[] = {(void*)&A, (void*)&L, (void*)&iters};
+    return cudaLaunchKernelExC(&cfg, fn, args);
 }
 
 template int cg_resident_configure<double>(int, int, int, const int32_t*, const int32_t*, const int32_t*,

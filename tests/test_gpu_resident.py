@@ -92,3 +92,24 @@ def test_resident_small_systems(m, n):
             assert g.stats()["cg_path_used"] == 3
         G = (A / d) @ A.T
         assert rel(x, np.linalg.solve(G, b)) < 1e-8
+
+
+@pytest.mark.parametrize("name,spec,seed", [("random 8000 x 24000", L.spec_random(8000, 24000, 5), 5),
+                                            ("mcf 48 x 48 x 4", L.spec_mcf(48, 4, 3), 6)])
+@pytest.mark.parametrize("fp32", [False, True])
+def test_resident_matrix_in_l2(name, spec, seed, fp32):
+    """Systems whose matrix slices do not fit in shared memory next to the
+    vectors (FP64 slices alone: 12 bytes x 2 nnz / 16 CTAs > 227 KB with the
+    8 m bytes of p) run the resident kernel with the matrix read from L2."""
+    lp = L.generate(spec, seed)
+    assert 8 * lp.m + 12 * 2 * lp.nnz / 16 > 227 * 1024 or fp32
+    rng = np.random.default_rng(seed)
+    d = np.exp(rng.uniform(-5, 5, lp.n))
+    b = rng.standard_normal(lp.m)
+    tol = 1e-5 if fp32 else 1e-10
+    kw = dict(pivots=16, cg_tol=tol, cg_max_iter=50000)
+    xr, itr, st = _cg(lp, d, b, "resident", fp32=fp32, **kw)
+    assert st["cg_path_used"] == 3
+    xg, itg, _ = _cg(lp, d, b, "graph", fp32=fp32, **kw)
+    assert abs(itr - itg) <= max(3, 0.02 * itg)
+    assert rel(xr, xg) < (1e-4 if fp32 else 1e-8)
