@@ -75,6 +75,7 @@ struct help_pcg {
     help_pcg_options opt;
     int device = 0;
     int num_sms = 0;
+    bool host_direct = false;  // kernels may access pageable host memory (Grace: host page tables)
     cudaStream_t stream = nullptr;
     std::string err;
 

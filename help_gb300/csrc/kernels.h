@@ -124,6 +124,8 @@ cudaError_t vec_add_f32(double* x, const float* e, int64_t n, cudaStream_t st); 
 cudaError_t vec_to_f32_scaled(const double* a, double scale, float* out, int64_t n, cudaStream_t st);
 cudaError_t vec_add_f32_scaled(double* x, const float* e, double scale, int64_t n, cudaStream_t st);
 cudaError_t vec_fill(double* x, double v, int64_t n, cudaStream_t st);
+// dst = src (either may be host memory the device reaches directly)
+cudaError_t vec_copy(const double* src, double* dst, int64_t n, int num_sms, cudaStream_t st);
 cudaError_t vec_fill_f32(float* x, float v, int64_t n, cudaStream_t st);
 // Deterministic sum of squares into out[0] (uses `part` of >= 1024 doubles).
 cudaError_t vec_sumsq(const double* x, int64_t n, double* part, double* out, cudaStream_t st);

@@ -151,6 +151,30 @@ cudaError_t vec_add_f32_scaled(double* x, const float* e, double scale, int64_t 
     k_add_f32_scaled<<<grid_for(n, 256), 256, 0, st>>>(x, e, scale, n);
     return cudaGetLastError();
 }
+namespace {
+__global__ void k_copy16(const double2* __restrict__ src, double2* __restrict__ dst, int64_t n2) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n2; i += (int64_t)gridDim.x * blockDim.x)
+        dst[i] = src[i];
+}
+__global__ void k_copy8(const double* __restrict__ src, double* __restrict__ dst, int64_t n) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        dst[i] = src[i];
+}
+}  // namespace
+
+cudaError_t vec_copy(const double* src, double* dst, int64_t n, int num_sms, cudaStream_t st) {
+    if (n <= 0) return cudaSuccess;
+    const int blocks = num_sms > 0 ? num_sms * 4 : 256;
+    if ((((uintptr_t)src | (uintptr_t)dst) & 15) == 0) {
+        const int64_t n2 = n / 2;
+        if (n2 > 0) k_copy16<<<blocks, 256, 0, st>>>(reinterpret_cast<const double2*>(src), reinterpret_cast<double2*>(dst), n2);
+        if (n & 1) k_copy8<<<1, 32, 0, st>>>(src + 2 * n2, dst + 2 * n2, 1);
+    } else {
+        k_copy8<<<blocks, 256, 0, st>>>(src, dst, n);
+    }
+    return cudaGetLastError();
+}
+
 cudaError_t vec_fill(double* x, double v, int64_t n, cudaStream_t st) {
     k_fill<<<grid_for(n, 256), 256, 0, st>>>(x, v, n);
     return cudaGetLastError();

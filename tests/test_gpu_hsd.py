@@ -54,3 +54,22 @@ def test_ipm_device_products_match_host_loops(name, spec, seed):
     assert a["iterations"] == b["iterations"]
     assert abs(a["primal_obj"] - b["primal_obj"]) <= 1e-9 * (1 + abs(b["primal_obj"]))
     assert a["rel_gap"] < 1e-8 and a["primal_infeas"] < 1e-7
+
+
+def test_host_arrays_at_8_byte_offsets():
+    """Host arrays that are not 16-byte aligned (the direct-copy path then
+    moves 8-byte words)."""
+    lp = L.generate(L.spec_random(300, 900, 5), 9)
+    rng = np.random.default_rng(9)
+    A = np.zeros((lp.m, lp.n))
+    for j in range(lp.n):
+        A[lp.row_ind[lp.col_ptr[j]:lp.col_ptr[j + 1]], j] = lp.val[lp.col_ptr[j]:lp.col_ptr[j + 1]]
+    xb = rng.standard_normal(lp.n + 1)
+    yb = np.zeros(lp.m + 1)
+    x, y = xb[1:], yb[1:]
+    assert x.ctypes.data % 16 == 8 or xb.ctypes.data % 16 == 8
+    with backend.GpuNormalEquations(pivots=4) as g:
+        g.LinearEquation_Construct(lp)
+        rc = g.lib.help_pcg_matvec(g.ctx, native.HELP_OP_A, native.ptr(x), native.ptr(y))
+        assert rc == native.HELP_OK
+    assert rel(y, A @ x) < 1e-13 and yb[0] == 0.0
