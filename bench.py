@@ -158,7 +158,7 @@ def cpu_adat_baseline(lp, d, seconds: float = 10.0) -> dict:
             "seconds": el}
 
 
-def ipm_run(config: int, precision: str, pivots: int | None = None) -> dict:
+def ipm_run(config: int, precision: str, pivots: int | None = None, lp=None, cg_path: str = "auto") -> dict:
     """HSD IPM (the reference's HSD_Main restated) to a 1e-8 gap on the GPU
     backend, with the FP64 residual ||rhs - G x_2|| / ||rhs|| of every Newton
     solve read back after the solve."""
@@ -166,11 +166,16 @@ def ipm_run(config: int, precision: str, pivots: int | None = None) -> dict:
 
     from help_gb300 import backend, hsd, native, lp as L
 
-    lp = L.make_lp(config, 0)
-    k = L.config_pivots(config) if pivots is None else min(pivots, lp.m)
+    name = None
+    if lp is None:
+        lp = L.make_lp(config, 0)
+        k = L.config_pivots(config) if pivots is None else min(pivots, lp.m)
+    else:
+        name, lp = lp
+        k = min(pivots, lp.m)
     solves = []
-    with backend.GpuNormalEquations(pivots=k, precision=precision, cg_tol=1e-10,
-                                    ir_tol=1e-10, cg_max_iter=1_000_000) as g:
+    with backend.GpuNormalEquations(pivots=k, precision=precision, cg_tol=1e-10, ir_tol=1e-10,
+                                    cg_max_iter=1_000_000, cg_path=cg_path) as g:
         lib, ctx = g.lib, g.ctx
 
         def solve(_c, d, b1, b2, x1, x2):
@@ -191,7 +196,7 @@ def ipm_run(config: int, precision: str, pivots: int | None = None) -> dict:
         wall = time.perf_counter() - t0
         st = g.stats()
     res = np.array([s_[0] for s_ in solves]) if solves else np.zeros(1)
-    return {"config": "config %d: m=%d n=%d nnz=%d" % (config, lp.m, lp.n, lp.nnz),
+    return {"config": "%s: m=%d n=%d nnz=%d" % (name or "config %d" % config, lp.m, lp.n, lp.nnz),
             "form": "%s PCG, k=%d, tol 1e-10, CG path %s" % (
                 "plain FP64" if precision == "fp64" else "FP32 CG in FP64 refinement", k,
                 {1: "graph", 2: "single cluster", 3: "resident cluster"}.get(int(st["cg_path_used"]), "?")),
@@ -214,6 +219,15 @@ def ipm_time(config: int = 0) -> dict:
     direct = ipm_run(config, "fp64", pivots=1 << 30)
     direct["obj_rel_diff_vs_fp64"] = abs(direct["primal_obj"] - plain["primal_obj"]) / abs(plain["primal_obj"])
     plain["direct"] = direct
+    # the multicommodity-flow family of config 3 at a size whose IPM finishes
+    # in seconds (24 x 24 grid, 4 commodities): the auto CG path (resident
+    # cluster) against the whole-GPU graph
+    from help_gb300 import lp as L
+    mcf = ("multicommodity flow 24 x 24 grid, 4 commodities (config 3's generator)",
+           L.generate(L.spec_mcf(24, 4, 3), 11))
+    m_auto = ipm_run(0, "fp64", pivots=16, lp=mcf)
+    m_graph = ipm_run(0, "fp64", pivots=16, lp=mcf, cg_path="graph")
+    plain["mcf"] = {"auto": m_auto, "graph": m_graph}
     return plain
 
 
