@@ -237,6 +237,7 @@ int run_pcg(help_pcg* ctx, V* x, V* r0, double tol, long long max_iter, int prec
     A.part_aw = part + 2 * nb;
     A.part_pq = part + 3 * nb;
     A.precond_only = precond_only;
+    A.stage_a = (A.k > 0 && A.k <= 8192 && ctx->nnz_c >= 4 * (int64_t)nb * A.k) ? 1 : 0;
     DevCtrl* c = ctrl_of(ctx);
     A.sc = &c->cg;
     // scalars the host sets: tolerance and cap (everything else the init kernel writes)

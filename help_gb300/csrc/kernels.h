@@ -61,6 +61,7 @@ struct CgArgs {
     double* part_aw;
     double* part_pq;
     int precond_only;  // stop after the first preconditioner application (z in p1)
+    int stage_a;       // k_p2 copies a into shared memory (k <= 8192, C large against blocks x k)
     CgScalars* sc;
 };
 
