@@ -158,10 +158,14 @@ def cpu_adat_baseline(lp, d, seconds: float = 10.0) -> dict:
             "seconds": el}
 
 
-def ipm_run(config: int, precision: str, pivots: int | None = None, lp=None, cg_path: str = "auto") -> dict:
+def ipm_run(config: int, precision: str, pivots: int | None = None, lp=None, cg_path: str = "auto",
+            oracle: bool = False) -> dict:
     """HSD IPM (the reference's HSD_Main restated) to a 1e-8 gap on the GPU
     backend, with the FP64 residual ||rhs - G x_2|| / ||rhs|| of every Newton
-    solve read back after the solve."""
+    solve read back after the solve.  oracle: every Newton system of the run
+    (d, b_1, b_2 and the solution) is recorded, and after the timed run each
+    is solved again by the FP64 direct form (pivots = m: the full Cholesky of
+    A D^-1 A^T, CG to 1e-14) to report the solutions' errors against it."""
     import ctypes as C
 
     from help_gb300 import backend, hsd, native, lp as L
@@ -174,6 +178,12 @@ def ipm_run(config: int, precision: str, pivots: int | None = None, lp=None, cg_
         name, lp = lp
         k = min(pivots, lp.m)
     solves = []
+    recorded = []  # (d, b1, b2, x1, x2) of every Newton solve, when oracle
+    m_, n_ = lp.m, lp.n
+
+    def host(ptr, count):
+        return np.ctypeslib.as_array(C.cast(ptr, C.POINTER(C.c_double)), (count,)).copy()
+
     with backend.GpuNormalEquations(pivots=k, precision=precision, cg_tol=1e-10, ir_tol=1e-10,
                                     cg_max_iter=1_000_000, cg_path=cg_path) as g:
         lib, ctx = g.lib, g.ctx
@@ -182,6 +192,8 @@ def ipm_run(config: int, precision: str, pivots: int | None = None, lp=None, cg_
             rc = lib.help_pcg_solve(ctx, d, b1, b2, x1, x2)
             st = g.stats()
             solves.append((st["rel_residual"], st["fell_back"], st["cg_iterations"], st["cg_iterations_fp32"]))
+            if oracle:
+                recorded.append((host(d, n_), host(b1, n_), host(b2, m_), host(x1, n_), host(x2, m_)))
             return rc
 
         fns = (native.CONSTRUCT_FN(lambda _c, m, n, cp, ri, v: lib.help_pcg_construct(ctx, m, n, cp, ri, v)),
@@ -195,6 +207,23 @@ def ipm_run(config: int, precision: str, pivots: int | None = None, lp=None, cg_
         r = hsd.solve_lp(lp, be)
         wall = time.perf_counter() - t0
         st = g.stats()
+    errs = None
+    if oracle and recorded:
+        ex, ey = [], []
+        with backend.GpuNormalEquations(pivots=lp.m, cg_tol=1e-14, cg_max_iter=1000) as o:
+            o.LinearEquation_Construct(lp)
+            last_d = None
+            for d, b1, b2, x1, x2 in recorded:
+                if last_d is None or not np.array_equal(d, last_d):
+                    o.RenewLinearEquation(d)
+                    last_d = d
+                ox1, ox2 = o.SolveLinearEquation(d, b1, b2)
+                ex.append(float(np.linalg.norm(x1 - ox1) / max(np.linalg.norm(ox1), 1e-300)))
+                ey.append(float(np.linalg.norm(x2 - ox2) / max(np.linalg.norm(ox2), 1e-300)))
+        errs = {"oracle": "FP64 direct form (pivots = m, full Cholesky of A D^-1 A^T, CG to 1e-14) on the "
+                          "recorded systems, after the timed run",
+                "dy_rel_err_max": max(ey), "dy_rel_err_median": float(np.median(ey)),
+                "dx_rel_err_max": max(ex), "dx_rel_err_median": float(np.median(ex))}
     res = np.array([s_[0] for s_ in solves]) if solves else np.zeros(1)
     return {"config": "%s: m=%d n=%d nnz=%d" % (name or "config %d" % config, lp.m, lp.n, lp.nnz),
             "form": "%s PCG, k=%d, tol 1e-10, CG path %s" % (
@@ -206,13 +235,14 @@ def ipm_run(config: int, precision: str, pivots: int | None = None, lp=None, cg_
             "cg_iterations_fp32": int(sum(s_[3] for s_ in solves)), "solves": len(solves),
             "solves_finished_in_fp64": int(sum(s_[1] for s_ in solves)),
             "newton_residual_max": float(res.max()), "newton_residual_median": float(np.median(res)),
-            "backend_seconds": round(r["backend_s"], 3)}
+            "backend_seconds": round(r["backend_s"], 3),
+            **({"newton_solution_errors": errs} if errs else {})}
 
 
 def ipm_time(config: int = 0) -> dict:
     """Plain FP64 IPM time, and the mixed form measured against it."""
-    plain = ipm_run(config, "fp64")
-    mixed = ipm_run(config, "mixed")
+    plain = ipm_run(config, "fp64", oracle=True)
+    mixed = ipm_run(config, "mixed", oracle=True)
     mixed["obj_rel_diff_vs_fp64"] = abs(mixed["primal_obj"] - plain["primal_obj"]) / abs(plain["primal_obj"])
     plain["mixed"] = mixed
     # direct form: every row a pivot, i.e. the full Cholesky of A D^-1 A^T
