@@ -52,8 +52,10 @@ namespace {
 constexpr int kResThreads = 256;
 constexpr int kResWarps = kResThreads / 32;
 
-// A CSR slice in shared memory: rows 0..rows-1 (row0 + r in the whole
-// matrix), ptr rebased to 0, column indices of the whole matrix.
+// A slice of rows of a CSR matrix: rows 0..rows-1 are rows row0 + r of the
+// whole matrix, column indices are the whole matrix's.  In shared memory
+// (load_rows: ptr rebased to 0) or read in place from HBM (global_rows: ptr
+// points at the whole matrix's row pointers from row0 on).
 template <class V>
 struct LocalCsr {
     const int* ptr;
