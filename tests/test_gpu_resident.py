@@ -113,3 +113,21 @@ def test_resident_matrix_in_l2(name, spec, seed, fp32):
     xg, itg, _ = _cg(lp, d, b, "graph", fp32=fp32, **kw)
     assert abs(itr - itg) <= max(3, 0.02 * itg)
     assert rel(xr, xg) < (1e-4 if fp32 else 1e-8)
+
+
+@pytest.mark.parametrize("name,spec,seed", [("smem matrix", L.spec_random(400, 1200, 5), 3),
+                                            ("L2 matrix", L.spec_random(8000, 24000, 5), 5)])
+def test_resident_repeatable(name, spec, seed):
+    """The same solve twice gives the same bits (every reduction in a fixed
+    order, no atomics on values)."""
+    lp = L.generate(spec, seed)
+    rng = np.random.default_rng(seed)
+    d = np.exp(rng.uniform(-5, 5, lp.n))
+    b = rng.standard_normal(lp.m)
+    with backend.GpuNormalEquations(pivots=16, cg_tol=1e-10, cg_max_iter=50000, cg_path="resident") as g:
+        g.LinearEquation_Construct(lp)
+        g.RenewLinearEquation(d)
+        x1, i1 = g.cg(b)
+        x2, i2 = g.cg(b)
+        assert g.stats()["cg_path_used"] == 3
+    assert i1 == i2 and np.array_equal(x1, x2)
