@@ -1101,17 +1101,6 @@ int help_pcg_matvec_acc(help_pcg* ctx, int32_t transpose, int32_t sign, const do
     return d2h(ctx, dest, ctx->x2.as<double>(), nout);
 }
 
-int help_exact_sum(const double* x, int32_t n, double* out3) {
-    if (!x || !out3 || n < 0 || n > 256) return HELP_E_ARG;
-    double* d = nullptr;
-    if (cudaMalloc(&d, sizeof(double) * 259) != cudaSuccess) return HELP_E_NOMEM;
-    cudaError_t e = cudaMemcpy(d, x, sizeof(double) * (size_t)n, cudaMemcpyHostToDevice);
-    if (e == cudaSuccess) e = exact_sum_test(d, n, d + 256, nullptr);
-    if (e == cudaSuccess) e = cudaMemcpy(out3, d + 256, sizeof(double) * 3, cudaMemcpyDeviceToHost);
-    cudaFree(d);
-    return e == cudaSuccess ? HELP_OK : HELP_E_CUDA;
-}
-
 int help_pcg_precond_apply(help_pcg* ctx, const double* r, double* z) {
     if (!ctx || !r || !z) return HELP_E_ARG;
     if (!ctx->renewed) return fail(ctx, HELP_E_ARG, "precond: renew first");

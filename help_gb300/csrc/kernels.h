@@ -125,9 +125,6 @@ cudaError_t vec_add_f32(double* x, const float* e, int64_t n, cudaStream_t st); 
 cudaError_t vec_to_f32_scaled(const double* a, double scale, float* out, int64_t n, cudaStream_t st);
 cudaError_t vec_add_f32_scaled(double* x, const float* e, double scale, int64_t n, cudaStream_t st);
 cudaError_t vec_fill(double* x, double v, int64_t n, cudaStream_t st);
-// exact sums (exactsum.cuh) of x[0, n), n <= 256: over a CTA, a half warp
-// (first 16) and a warp with three values per lane (first 96)
-cudaError_t exact_sum_test(const double* x, int n, double* out, cudaStream_t st);
 // dst = src (either may be host memory the device reaches directly)
 cudaError_t vec_copy(const double* src, double* dst, int64_t n, int num_sms, cudaStream_t st);
 cudaError_t vec_fill_f32(float* x, float v, int64_t n, cudaStream_t st);

@@ -3,7 +3,6 @@
 // D^-1 (b_1 - A^T x_2) of UsePCG_CPU.cpp:103-177, the FP64 residual of the
 // refinement loop) and small vector kernels.
 #include "common.cuh"
-#include "exactsum.cuh"
 #include "kernels.h"
 #include "spmv.cuh"
 
@@ -162,34 +161,6 @@ __global__ void k_copy8(const double* __restrict__ src, double* __restrict__ dst
         dst[i] = src[i];
 }
 }  // namespace
-
-namespace {
-// One CTA of 256 threads: out[0] = exact sum of x[0, n) over the block,
-// out[1] = of x[0, min(n, 16)) over a half warp, out[2] = of x[0, min(n, 96))
-// over a warp holding three values per lane.
-__global__ void __launch_bounds__(256) k_exact_sum(const double* __restrict__ x, int n, double* __restrict__ out) {
-    __shared__ ExactScratch s;
-    const int t = threadIdx.x;
-    const double v = t < n ? x[t] : 0.0;
-    const double b = block_sum_exact(v, &s);
-    if (t == 0) out[0] = b;
-    if (t < 32) {
-        const double h = group_sum_exact<16>(t < 16 ? v : 0.0);
-        const double w3[3] = {t < n ? x[t] : 0.0, t + 32 < n && t + 32 < 96 ? x[t + 32] : 0.0,
-                              t + 64 < n && t + 64 < 96 ? x[t + 64] : 0.0};
-        const double w = group_sum_exact<32, 3>(w3);
-        if (t == 0) {
-            out[1] = h;
-            out[2] = w;
-        }
-    }
-}
-}  // namespace
-
-cudaError_t exact_sum_test(const double* x, int n, double* out, cudaStream_t st) {
-    k_exact_sum<<<1, 256, 0, st>>>(x, n, out);
-    return cudaGetLastError();
-}
 
 cudaError_t vec_copy(const double* src, double* dst, int64_t n, int num_sms, cudaStream_t st) {
     if (n <= 0) return cudaSuccess;

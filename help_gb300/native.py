@@ -178,7 +178,6 @@ GPU_SYMBOLS = [
     "help_pcg_default_options", "help_pcg_create", "help_pcg_free", "help_pcg_construct",
     "help_pcg_renew", "help_pcg_solve", "help_pcg_destruct", "help_pcg_get_stats",
     "help_pcg_last_error", "help_pcg_matvec", "help_pcg_matvec_dev", "help_pcg_matvec_acc", "help_pcg_precond_apply",
-    "help_exact_sum",
     "help_pcg_get_pivots", "help_pcg_cg", "help_pcg_cg_f32", "help_adat_assemble", "help_adat_matvec_noalloc",
     "help_mlp_create", "help_mlp_free", "help_mlp_last_error", "help_mlp_set_params", "help_mlp_get_params",
     "help_mlp_forward", "help_mlp_loss_grad", "help_mlp_train_step", "help_pcg_attach_mlp", "help_pcg_features",
@@ -222,7 +221,6 @@ def gpu_lib() -> C.CDLL:
         lib.help_pcg_matvec.argtypes = [vp, i32, dp, dp]
         lib.help_pcg_matvec_dev.argtypes = [vp, i32, i32, vp, vp, vp]
         lib.help_pcg_matvec_acc.argtypes = [vp, i32, i32, dp, dp]
-        lib.help_exact_sum.argtypes = [dp, i32, dp]
         lib.help_pcg_precond_apply.argtypes = [vp, dp, dp]
         lib.help_pcg_get_pivots.argtypes = [vp, dp, dp, dp]
         lib.help_pcg_cg.argtypes = [vp, dp, dp, C.POINTER(C.c_int64)]

@@ -153,11 +153,6 @@ int help_pcg_matvec_dev(help_pcg* ctx, int32_t op, int32_t fp32, const void* x, 
  * optional matvec of its backend table.  Each row's products are summed on
  * the device and added to dest once. */
 int help_pcg_matvec_acc(help_pcg* ctx, int32_t transpose, int32_t sign, const double* v, double* dest);
-/* The exact sums behind the resident CG's reductions (fixed-point on the
- * integer pipes, one rounding to nearest), for tests: out3[0] = sum of x[0, n)
- * over one CTA, out3[1] = of the first 16 over a half warp, out3[2] = of the
- * first 96 over a warp holding three per lane.  n <= 256, host arrays. */
-int help_exact_sum(const double* x, int32_t n, double* out3);
 /* z = M^-1 r with the last renew's partial-Cholesky preconditioner
  * (Preconditioner, PCG.cpp:183-196), vectors in the original row order. */
 int help_pcg_precond_apply(help_pcg* ctx, const double* r, double* z);
