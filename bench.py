@@ -316,8 +316,9 @@ def spmv_large(steps: int, warmup: int, local: int) -> dict:
                 times.append(time.perf_counter() - t0)
                 assert rc == native.HELP_OK
             hp[name + "_ms"] = round(1e3 * float(np.median(times[1:])), 2)
-        out["hsd_products"] = dict(hp, note="wall time per call through the C ABI with host buffers "
-                                            "(H2D of v and dest, SpMV, D2H), median of 3 after 1 warm-up")
+        out["hsd_products"] = dict(hp, note="wall time per call through the C ABI with host buffers (v and "
+                                            "dest read from the host arrays, one SpMV pass storing into dest), "
+                                            "median of 3 after 1 warm-up")
     return out
 
 
