@@ -38,6 +38,9 @@
 #include <cooperative_groups.h>
 
 #include <algorithm>
+#include <map>
+#include <mutex>
+#include <utility>
 
 #include "common.cuh"
 #include "kernels.h"
@@ -626,6 +629,24 @@ ResLayout resident_layout(int m, int n, int k, int cs, int vbytes, const int32_t
 
 // The kernel for a layout: FP64 always exchanges t through L2 (measured
 // faster), FP32 through shared memory where t fits there.
+// The dynamic shared-memory limit is a property of the function (per
+// device), shared by every context in the process: only ever raise it, so a
+// context sizing a smaller system never lowers the limit under another
+// context's launch.
+static cudaError_t raise_smem_limit(const void* fn, int bytes) {
+    static std::mutex mu;
+    static std::map<std::pair<const void*, int>, int> limit;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    std::lock_guard<std::mutex> lock(mu);
+    int& cur = limit[{fn, dev}];
+    if (bytes <= cur) return cudaSuccess;
+    e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    if (e == cudaSuccess) cur = bytes;
+    return e;
+}
+
 template <class V>
 const void* resident_fn(bool mat_smem, bool t_smem) {
     if constexpr (sizeof(V) == 8) {
@@ -661,7 +682,7 @@ int cg_resident_configure(int m, int n, int k, const int32_t* rp, const int32_t*
         for (int cs : {16, 8}) {
             const ResLayout lay = resident_layout(m, n, k, cs, (int)sizeof(V), rp, cp, crp, mat_smem, t_smem);
             if (lay.total + static_bytes > (size_t)optin) continue;
-            if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lay.total) != cudaSuccess) {
+            if (raise_smem_limit(fn, (int)lay.total) != cudaSuccess) {
                 cudaGetLastError();
                 continue;
             }
@@ -685,10 +706,8 @@ int cg_resident_configure(int m, int n, int k, const int32_t* rp, const int32_t*
 // Up to `iters` CG iterations in one launch of one cluster of `cs` CTAs.
 template <class V>
 cudaError_t cg_launch_resident(const CgArgs<V>& A, const ResLayout& L, int cs, int iters, cudaStream_t st) {
-    // the shared-memory limit is a property of the function, shared by every
-    // context: set it to this context's size before each launch
     const void* fn = resident_fn<V>(L.mat_smem != 0, L.t_smem != 0);
-    cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.total);
+    const cudaError_t e = raise_smem_limit(fn, (int)L.total);
     if (e != cudaSuccess) return e;
     cudaLaunchAttribute at[1];
     cudaLaunchConfig_t cfg = resident_config(cs, L.total, st, at);
