@@ -372,9 +372,12 @@ def learned_ablation() -> dict:
         c = learned.evaluate(lp, 16, learned.fixed_warm_params())
         dh = learned.evaluate(lp, 16, learned.diag_head_only(params))
         wh = learned.evaluate(lp, 16, learned.warm_head_only(params))
+        lm = learned.evaluate(lp, 16, params, precision="mixed")  # learned + mixed, the benchmark's chosen form
         runs.append({"seed": s, "cg_plain": a["cg_iterations"], "cg_learned": b["cg_iterations"],
                      "cg_fixed_warm_start": c["cg_iterations"], "cg_learned_diag_head_only": dh["cg_iterations"],
                      "cg_learned_warm_head_only": wh["cg_iterations"],
+                     "cg_learned_mixed": lm["cg_iterations"], "s_learned_mixed": round(lm["seconds"], 3),
+                     "obj_rel_diff_learned_mixed": abs(lm["primal_obj"] - a["primal_obj"]) / abs(a["primal_obj"]),
                      "s_plain": round(a["seconds"], 3), "s_learned": round(b["seconds"], 3),
                      "obj_rel_diff": abs(a["primal_obj"] - b["primal_obj"]) / abs(a["primal_obj"]),
                      "fallbacks": b["learned_fallbacks"]})

@@ -359,12 +359,15 @@ def train(data: dict, steps: int = 600, lr: float = 3e-3, seed: int = 0, device:
     return params, losses
 
 
-def evaluate(lp, pivots: int, params: np.ndarray | None, cg_tol: float = 1e-10, device: int = 0) -> dict:
-    """One IPM run; with ``params`` the model is attached."""
+def evaluate(lp, pivots: int, params: np.ndarray | None, cg_tol: float = 1e-10, device: int = 0,
+             precision: str = "fp64") -> dict:
+    """One IPM run; with ``params`` the model is attached; precision "mixed"
+    runs the FP32-in-FP64-refinement form (refined to cg_tol)."""
     from . import hsd
 
     mlp = Mlp(device, params) if params is not None else None
-    with GpuNormalEquations(pivots=pivots, cg_tol=cg_tol, cg_max_iter=200_000, device=device) as ne:
+    with GpuNormalEquations(pivots=pivots, cg_tol=cg_tol, cg_max_iter=200_000, device=device,
+                            precision=precision, ir_tol=cg_tol) as ne:
         if mlp is not None:
             ne._check(ne.lib.help_pcg_attach_mlp(ne.ctx, mlp.h))
         t0 = time.perf_counter()

@@ -81,3 +81,19 @@ def test_ipm_with_model_matches_plain(trained):
     print(json.dumps([{"seed": r["seed"], "cg_plain": r["plain"]["cg_iterations"],
                        "cg_learned": r["learned"]["cg_iterations"],
                        "cg_fixed_warm_start": r["fixed_warm_start"]["cg_iterations"]} for r in report]))
+
+
+def test_ipm_learned_mixed_matches_plain(trained):
+    """The learned part with the mixed form (FP32 CG inside FP64 refinement):
+    the same optimum as the plain FP64 PCG (1e-6 relative in the objective),
+    the model's correction applied to both precisions' Schur diagonals."""
+    from help_gb300 import learned
+
+    params, _ = trained
+    for s in TEST_SEEDS[:2]:
+        lp = L.generate(L.spec_mcf(**SPEC), s)
+        plain = learned.evaluate(lp, PIVOTS, None)
+        lm = learned.evaluate(lp, PIVOTS, params, precision="mixed")
+        assert plain["status"] == 0 and lm["status"] == 0
+        assert abs(plain["primal_obj"] - lm["primal_obj"]) / abs(plain["primal_obj"]) < 1e-6
+        assert lm["rel_gap"] < 1e-8
