@@ -85,6 +85,8 @@ def test_free_layout_rows_slacks_and_dropped_entries(tmp_path):
     (FREE.replace(" N  obj\n", "").replace(" N  freerow\n", ""), "objective"),
     (FREE.replace("4.0 r2 10.0", "4.0 r2 1O.0"), "bad value"),
     (FREE.replace(" E  r1", " X  r1"), "row type"),
+    ("OBJSENSE\n    MAX\n" + FREE, "OBJSENSE"),
+    (FREE.replace("COLUMNS\n", "COLUMNS\n x9 r1\n"), "COLUMNS"),
 ])
 def test_mps_errors(tmp_path, text, why):
     p = tmp_path / "bad.mps"
@@ -124,3 +126,11 @@ def test_hsd_on_an_mps_read_instance_matches_the_generated_one(tmp_path):
     r2 = hsd.solve_lp(back, ob.OracleNormalEquations(pivots=4, tol=1e-14, max_iter=10**6).ne_backend())
     assert r1["status"] == r2["status"] == 0
     assert r1["primal_obj"] == r2["primal_obj"] and r1["iterations"] == r2["iterations"]
+
+
+def test_rhs_on_the_objective_row_is_ignored(tmp_path):
+    """An RHS entry on the objective row (a constant offset) does not enter b."""
+    p = tmp_path / "o.mps"
+    p.write_text(FREE.replace(" r3 1.0\n", " r3 1.0\n rhs obj 5.0\n"))
+    lp = L.read_mps(str(p))
+    assert np.array_equal(lp.b, [4.0, 10.0, 1.0])
