@@ -5,10 +5,11 @@
 // one is UsePCG_CPU.cpp + PCG.cpp.  Build the reference with this file in
 // their place and link libhelp_gpu.so:
 //
-//   g++ -O2 -fopenmp -I<HELP sources> -I<this repo>/include \
-//       Crushing.cpp GlobalVar.cpp Hash.cpp Helper.cpp HSDSolver.cpp Init.cpp \
-//       Main.cpp MPSRead.cpp Presolve.cpp Report.cpp UsePCG_GPU.cpp \
+//   g++ -O2 -fopenmp -I<HELP sources> -I<this repo>/include
+//       Crushing.cpp GlobalVar.cpp Hash.cpp Helper.cpp HSDSolver.cpp Init.cpp
+//       Main.cpp MPSRead.cpp Presolve.cpp Report.cpp UsePCG_GPU.cpp
 //       -L<this repo>/help_gb300/_lib -lhelp_gpu -Wl,-rpath,<...>
+//   (one command line)
 //
 // MPSRead, Crushing, Presolve, the HSD iteration and Report are unchanged.
 // The matrix is read from the same globals UsePCG_CPU.cpp reads

@@ -207,8 +207,10 @@ int run_pcg(help_pcg* ctx, V* x, V* r0, double tol, long long max_iter, int prec
     const bool f32 = std::is_same<V, float>::value;
     const int slot = f32 ? 1 : 0;
     const int nb = ctx->cg_blocks;
+    // zero every byte, padding included: the graph below is re-captured when
+    // these bytes change
     CgArgs<V> A;
-    std::memset(&A, 0, sizeof(A));
+    std::memset(static_cast<void*>(&A), 0, sizeof(A));
     A.m = ctx->m;
     A.n = ctx->n;
     A.k = ctx->k;
