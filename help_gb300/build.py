@@ -30,7 +30,7 @@ GPU_CU = ["api.cu", "pcg.cu", "pcg_resident.cu", "renew.cu", "dense.cu", "vec.cu
           "learned.cu", "mlp_api.cu"]
 GPU_CPP = ["items.cpp"]
 GPU_HDR = ["common.cuh", "spmv.cuh", "kernels.h", "context.h", "items.h", "mlp.h"]
-LP_CPP = ["lp_gen.cpp", "hsd.cpp", "lp_io.cpp"]
+LP_CPP = ["lp_gen.cpp", "hsd.cpp", "lp_io.cpp", "lindep.cpp"]
 
 
 def _newer(target: str, deps: list[str]) -> bool:

@@ -373,8 +373,10 @@ int gen_block(const help_lp_spec* s, uint64_t seed, help_lp* out) {
 
 // Multicommodity flow on a G x G grid with 4-neighbour bidirectional arcs.
 // Rows: per commodity the node-balance rows of nodes 1..N-1 (node 0 is
-// grounded: each commodity's incidence matrix has rank N-1), then one 'L'
-// capacity row per arc.  Columns: flow (commodity, arc) with +1 at the tail
+// grounded: each commodity's incidence matrix has rank N-1), or of all N
+// nodes with mcf_ungrounded (then each commodity's rows sum to zero and A is
+// K rows short of full rank, as the reference's inputs are when its
+// dependent-row presolve is needed), then one 'L' capacity row per arc.  Columns: flow (commodity, arc) with +1 at the tail
 // row, -1 at the head row and +1 at the arc's capacity row; then one slack
 // column per capacity row (Crushing.cpp:71-99 adds these for 'L' rows).
 // Demands come from routing, per commodity, `pairs` random source/sink pairs
@@ -400,7 +402,8 @@ int gen_mcf(const help_lp_spec* s, uint64_t seed, help_lp* out) {
             }
         }
     const int32_t A = (int32_t)tail.size();
-    const int64_t m64 = (int64_t)K * (N - 1) + A;
+    const int32_t NR = s->mcf_ungrounded ? N : N - 1;  // node rows per commodity
+    const int64_t m64 = (int64_t)K * NR + A;
     const int64_t n64 = (int64_t)K * A + A;
     if (m64 > 2000000000LL || n64 > 2000000000LL) return -1;
     const int32_t m = (int32_t)m64, n = (int32_t)n64;
@@ -438,6 +441,7 @@ int gen_mcf(const help_lp_spec* s, uint64_t seed, help_lp* out) {
     if (rc) return rc;
     out->n_struct = K * A;
     auto node_row = [&](int32_t k, int32_t node) -> int32_t {
+        if (s->mcf_ungrounded) return k * N + node;
         return node == 0 ? -1 : k * (N - 1) + (node - 1);
     };
     int64_t p = 0;
@@ -451,7 +455,7 @@ int gen_mcf(const help_lp_spec* s, uint64_t seed, help_lp* out) {
             const int32_t rt = node_row(k, tail[a]), rh = node_row(k, head[a]);
             if (rt >= 0) { rr[cnt] = rt; vv[cnt++] = 1.0; }
             if (rh >= 0) { rr[cnt] = rh; vv[cnt++] = -1.0; }
-            rr[cnt] = K * (N - 1) + a;
+            rr[cnt] = K * NR + a;
             vv[cnt++] = 1.0;
             // sort the (at most 3) rows
             for (int x = 0; x < cnt; ++x)
@@ -468,7 +472,7 @@ int gen_mcf(const help_lp_spec* s, uint64_t seed, help_lp* out) {
     for (int32_t a = 0; a < A; ++a) {
         const int32_t j = K * A + a;
         out->col_ptr[j] = (int32_t)p;
-        out->row_ind[p] = K * (N - 1) + a;
+        out->row_ind[p] = K * NR + a;
         out->val[p] = 1.0;
         ++p;
         out->c[j] = 0.0;
@@ -476,13 +480,13 @@ int gen_mcf(const help_lp_spec* s, uint64_t seed, help_lp* out) {
     out->col_ptr[n] = (int32_t)p;
     out->nnz = p;
     for (int32_t k = 0; k < K; ++k)
-        for (int32_t node = 1; node < N; ++node)
+        for (int32_t node = s->mcf_ungrounded ? 0 : 1; node < N; ++node)
             out->b[node_row(k, node)] = q6(supply[(size_t)k * N + node]);
     for (int32_t a = 0; a < A; ++a) {
         double tot = 0.0;
         for (int32_t k = 0; k < K; ++k) tot += flow[(size_t)k * A + a];
-        out->b[K * (N - 1) + a] = q6(tot + g.uniform_range(1.0, 10.0));
-        out->row_type[K * (N - 1) + a] = 'L';
+        out->b[K * NR + a] = q6(tot + g.uniform_range(1.0, 10.0));
+        out->row_type[K * NR + a] = 'L';
     }
     return 0;
 }

@@ -83,9 +83,9 @@ def spec_zipf(m: int, n: int, k: int, s: float = 1.3, offset: int = 70) -> nativ
     return native.LpSpec(kind=native.HELP_LP_ZIPF, m=m, n=n, nnz_per_col=k, zipf_s=s, zipf_offset=offset)
 
 
-def spec_mcf(grid: int, commodities: int, pairs: int = 4) -> native.LpSpec:
+def spec_mcf(grid: int, commodities: int, pairs: int = 4, grounded: bool = True) -> native.LpSpec:
     return native.LpSpec(kind=native.HELP_LP_MCF, grid=grid, commodities=commodities,
-                         pairs_per_commodity=pairs)
+                         pairs_per_commodity=pairs, mcf_ungrounded=0 if grounded else 1)
 
 
 def spec_block(blocks: int, block_rows: int, block_cols: int, k: int, link_rows: int,
@@ -140,6 +140,39 @@ def read_mps(path: str) -> LP:
     if rc != 0:
         raise ValueError("help_lp_read_mps failed (%d): %s" % (rc, lib.help_lp_last_error().decode()))
     return _from_struct(lib, s, path)
+
+
+class PresolveNotApplicable(ValueError):
+    """The dependent-row presolve gave up: its elimination fills in past its
+    limits (random sparse matrices at 10^5 rows); solve the LP as it is."""
+
+
+def remove_dependent_rows(lp: LP, tol: float = 1e-8):
+    """(reduced LP, mask of the removed rows): the rows that are linear
+    combinations of the other rows dropped (help_lp_remove_dependent_rows;
+    the purpose of the reference's Presolve_Lindep.cpp:316).  Raises
+    ValueError when b disagrees with a dependency (primal infeasible) and
+    PresolveNotApplicable when the elimination passes its fill or work limit."""
+    lib = native.lp_lib()
+    s = native.LpStruct()
+    removed = np.zeros(lp.m, np.int32)
+    st = lp.as_struct()
+    rc = lib.help_lp_remove_dependent_rows(C.byref(st), tol, C.byref(s), native.ptr(removed))
+    if rc == -4:
+        raise PresolveNotApplicable("help_lp_remove_dependent_rows (-4): the elimination passed its fill or "
+                                    "work limit; no rows removed")
+    if rc < 0:
+        why = {-3: "primal infeasible: b disagrees with a dependent row", -2: "out of memory"}.get(rc, "bad arguments")
+        raise ValueError("help_lp_remove_dependent_rows failed (%d): %s" % (rc, why))
+    return _from_struct(lib, s, lp.name), removed.astype(bool)
+
+
+def expand_duals(y_reduced: np.ndarray, removed: np.ndarray) -> np.ndarray:
+    """Duals of the original LP from those of the reduced one: a dropped row is
+    a combination of kept rows, so y = 0 there keeps A^T y and b^T y."""
+    y = np.zeros(len(removed))
+    y[~np.asarray(removed, bool)] = y_reduced
+    return y
 
 
 def read_bin(path: str) -> LP:

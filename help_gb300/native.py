@@ -104,6 +104,7 @@ class LpSpec(C.Structure):
         ("block_cols", C.c_int32),
         ("link_rows", C.c_int32),
         ("link_prob", C.c_double),
+        ("mcf_ungrounded", C.c_int32),
     ]
 
 
@@ -184,7 +185,7 @@ GPU_SYMBOLS = [
 ]
 LP_SYMBOLS = [
     "help_lp_generate", "help_lp_free", "help_lp_write_mps", "help_csc_to_csr", "help_lp_read_mps",
-    "help_lp_write_bin", "help_lp_read_bin", "help_lp_last_error",
+    "help_lp_write_bin", "help_lp_read_bin", "help_lp_last_error", "help_lp_remove_dependent_rows",
     "help_hsd_default_options", "help_hsd_solve",
 ]
 
@@ -255,6 +256,8 @@ def lp_lib() -> C.CDLL:
         lib.help_lp_read_mps.argtypes = [C.c_char_p, C.POINTER(LpStruct)]
         lib.help_lp_write_bin.argtypes = [C.POINTER(LpStruct), C.c_char_p]
         lib.help_lp_read_bin.argtypes = [C.c_char_p, C.POINTER(LpStruct)]
+        lib.help_lp_remove_dependent_rows.argtypes = [C.POINTER(LpStruct), C.c_double, C.POINTER(LpStruct),
+                                                      C.c_void_p]
         lib.help_lp_last_error.argtypes = []
         lib.help_lp_last_error.restype = C.c_char_p
         lib.help_csc_to_csr.argtypes = [C.c_int32, C.c_int32] + [C.c_void_p] * 6

@@ -34,6 +34,8 @@ typedef struct help_lp_spec {
     int32_t pairs_per_commodity;    /* MCF: source/sink pairs routed per commodity  */
     int32_t blocks, block_rows, block_cols, link_rows;  /* BLOCK                    */
     double link_prob;               /* BLOCK: P(column appears in a linking row)    */
+    int32_t mcf_ungrounded;         /* MCF: keep every node row (rank K short); 0
+                                       grounds node 0 of each commodity            */
 } help_lp_spec;
 
 /*
@@ -85,6 +87,20 @@ int help_lp_read_mps(const char* path, help_lp* out);
  * row_type (m bytes), little-endian.  Return codes as help_lp_read_mps. */
 int help_lp_write_bin(const help_lp* lp, const char* path);
 int help_lp_read_bin(const char* path, help_lp* out);
+
+/* Linear-dependency presolve (the purpose of the reference's
+ * Presolve_Lindep.cpp:316, off there by default, LP.h:72): *out gets in
+ * without the rows that are linear combinations of the other rows, after
+ * checking that b agrees to 1e-8 relative.  A row is dependent when sparse
+ * elimination (Markowitz order, threshold pivoting) leaves none of its
+ * entries above tol x its largest entry (the reference's TOLAPIV is 1e-8);
+ * past a fill or work limit the last <= 4096 rows finish densely.  removed
+ * (m flags, may be NULL) marks the dropped rows.  Returns the number of rows
+ * dropped, -1 bad arguments, -2 out of memory, -3 b disagrees (the LP is
+ * primal infeasible), -4 the presolve does not apply: elimination fills in
+ * past 4 x nnz + 16 m entries or 64 x nnz + 2^28 entry updates with more
+ * than 4096 rows left (random sparse A at 10^5 rows), *out left empty. */
+int help_lp_remove_dependent_rows(const help_lp* in, double tol, help_lp* out, int32_t* removed);
 
 /* Message of the last failed read on this thread ("" if none). */
 const char* help_lp_last_error(void);
