@@ -385,6 +385,31 @@ def learned_ablation() -> dict:
             "loss_first": losses[0], "loss_last": losses[-1], "held_out": runs}
 
 
+def presolve_time() -> dict:
+    """The host dependent-row presolve (help_lp_remove_dependent_rows, one
+    thread): the 200 x 200 grid, 8-commodity flow with every node row kept
+    (eight rows short of full rank), and the random config-1 matrix, for
+    which it reports that it does not apply."""
+    from help_gb300 import lp as L
+
+    out = {"cores": 1}
+    lp = L.generate(L.spec_mcf(200, 8, grounded=False), 0)
+    t = time.perf_counter()
+    _, removed = L.remove_dependent_rows(lp)
+    out["mcf_200x200x8_ungrounded"] = {"rows": lp.m, "nnz": lp.nnz, "rows_removed": int(removed.sum()),
+                                       "s": round(time.perf_counter() - t, 3)}
+    lp1 = L.make_lp(1, 0)
+    t = time.perf_counter()
+    try:
+        _, removed = L.remove_dependent_rows(lp1)
+        result = "%d rows removed" % int(removed.sum())
+    except L.PresolveNotApplicable:
+        result = "not applicable (fill past the limits)"
+    out["config1_random"] = {"rows": lp1.m, "nnz": lp1.nnz, "result": result,
+                             "s": round(time.perf_counter() - t, 3)}
+    return out
+
+
 def run_reference(args) -> None:
     ws, rank, _ = dist_env()
     if rank != 0:
@@ -559,6 +584,10 @@ def main() -> None:
                 extra["learned"] = learned_ablation()
             except Exception as e:
                 extra["learned"] = {"error": str(e)}
+            try:
+                extra["presolve"] = presolve_time()
+            except Exception as e:
+                extra["presolve"] = {"error": str(e)}
     g.close()
     if rank == 0:
         extra["pcg"] = {}

@@ -26,3 +26,17 @@ def test_reference_arm_json_line():
     e2e = d["e2e"]
     assert e2e["value"] == d["value"] and e2e["h2d_bytes_per_step"] == 0 and e2e["d2h_bytes_per_step"] == 0
     assert "workload" in d["config"]
+
+
+def test_presolve_entry():
+    """The bench line's presolve entry (host code, timed on the host CPU):
+    eight rows off the ungrounded flow, not applicable to config 1."""
+    sys.path.insert(0, ROOT)
+    import bench
+
+    d = bench.presolve_time()
+    json.dumps(d)
+    assert d["mcf_200x200x8_ungrounded"]["rows_removed"] == 8
+    assert d["mcf_200x200x8_ungrounded"]["rows"] == 479200
+    assert d["config1_random"]["result"].startswith("not applicable")
+    assert d["mcf_200x200x8_ungrounded"]["s"] > 0 and d["config1_random"]["s"] > 0

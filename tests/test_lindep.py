@@ -159,3 +159,22 @@ def test_random_10k_rows_beyond_limits():
     with pytest.raises(L.PresolveNotApplicable):
         L.remove_dependent_rows(lp)
     assert time.perf_counter() - t < 30.0
+
+
+def test_ungrounded_flow_presolved_then_solved_by_hsd():
+    """The whole flow on the host: presolve, then the HSD driver over the
+    oracle's normal-equations backend reaches the grounded instance's
+    optimum, and its x is feasible for the full (unreduced) rows too."""
+    from help_gb300 import hsd
+    from oracle import bindings as ob
+
+    full = L.generate(L.spec_mcf(8, 3, 2, grounded=False), 4)
+    grounded = L.generate(L.spec_mcf(8, 3, 2), 4)
+    red, removed = L.remove_dependent_rows(full)
+    assert removed.sum() == 3
+    runs = [hsd.solve_lp(lp, ob.OracleNormalEquations(pivots=10, tol=1e-14, max_iter=10**6).ne_backend(),
+                         want_solution=True) for lp in (red, grounded)]
+    assert all(r["status"] == 0 and r["rel_gap"] < 1e-8 for r in runs)
+    assert abs(runs[0]["primal_obj"] - runs[1]["primal_obj"]) <= 1e-7 * (1 + abs(runs[1]["primal_obj"]))
+    x = runs[0]["x"]
+    assert np.linalg.norm(dense(full) @ x - full.b) <= 1e-7 * (1 + np.linalg.norm(full.b))
