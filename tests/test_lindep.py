@@ -178,3 +178,22 @@ def test_ungrounded_flow_presolved_then_solved_by_hsd():
     assert abs(runs[0]["primal_obj"] - runs[1]["primal_obj"]) <= 1e-7 * (1 + abs(runs[1]["primal_obj"]))
     x = runs[0]["x"]
     assert np.linalg.norm(dense(full) @ x - full.b) <= 1e-7 * (1 + np.linalg.norm(full.b))
+
+
+def test_bad_arguments_rejected():
+    """Non-positive tol, or an LP with no rows or columns: -1, nothing allocated."""
+    import ctypes as C
+
+    from help_gb300 import native
+
+    lib = native.lp_lib()
+    lp = L.generate(L.spec_random(20, 60, 3), 1)
+    out = native.LpStruct()
+    st = lp.as_struct()
+    for tol in (0.0, -1e-8, float("nan")):
+        assert lib.help_lp_remove_dependent_rows(C.byref(st), tol, C.byref(out), None) == -1
+    empty = native.LpStruct()
+    assert lib.help_lp_remove_dependent_rows(C.byref(empty), 1e-8, C.byref(out), None) == -1
+    assert lib.help_lp_remove_dependent_rows(None, 1e-8, C.byref(out), None) == -1
+    with pytest.raises(ValueError, match="bad arguments"):
+        L.remove_dependent_rows(lp, tol=0.0)
