@@ -6,7 +6,9 @@ owned by Python).  The five configurations are the benchmark's:
 * ``0`` random sparse LP, m=2,000, n=6,000, 5 nonzeros per column;
 * ``1`` same generator, m=100,000, n=400,000, 8 per column (k=512 pivots);
 * ``2`` Zipf(1.3) row law, m=500,000, n=2,000,000, 6 per column (k=1,024);
-* ``3`` multicommodity flow, 200x200 grid, 8 commodities;
+* ``3`` multicommodity flow, 200x200 grid, 8 commodities: every node row
+  (479,200 rows, each commodity's rows summing to zero), then the
+  dependent-row presolve removes one row per commodity (479,192 rows);
 * ``4`` block-angular: 32 blocks of 60,000 x 250,000 (5 per column) plus
   4,000 linking rows with P(column in row) = 0.002 (k=2,048).
 
@@ -99,7 +101,7 @@ CONFIGS = {
     0: (lambda: spec_random(2000, 6000, 5), 10),
     1: (lambda: spec_random(100_000, 400_000, 8), 512),
     2: (lambda: spec_zipf(500_000, 2_000_000, 6), 1024),
-    3: (lambda: spec_mcf(200, 8), 512),
+    3: (lambda: spec_mcf(200, 8, grounded=False), 512),
     4: (lambda: spec_block(32, 60_000, 250_000, 5, 4000, 0.002), 2048),
 }
 
@@ -185,9 +187,19 @@ def read_bin(path: str) -> LP:
     return _from_struct(lib, s, path)
 
 
+# Configurations generated rank-deficient and passed through the dependent-row
+# presolve, as HELP does with PRESOLVE_LINDEP set (Presolve.cpp:1254-1260)
+PRESOLVED = {3}
+
+
 def make_lp(config: int, seed: int = 0) -> LP:
     spec_fn, _ = CONFIGS[config]
-    return generate(spec_fn(), seed, name="config%d-seed%d" % (config, seed))
+    name = "config%d-seed%d" % (config, seed)
+    lp = generate(spec_fn(), seed, name=name)
+    if config in PRESOLVED:
+        lp, _ = remove_dependent_rows(lp)
+        lp.name = name
+    return lp
 
 
 def config_pivots(config: int) -> int:

@@ -197,3 +197,11 @@ def test_bad_arguments_rejected():
     assert lib.help_lp_remove_dependent_rows(None, 1e-8, C.byref(out), None) == -1
     with pytest.raises(ValueError, match="bad arguments"):
         L.remove_dependent_rows(lp, tol=0.0)
+
+
+def test_config3_generated_full_then_presolved():
+    """Config 3 as specified: every node row (479,200), one per commodity
+    removed by the presolve, leaving 479,192 rows and every column."""
+    lp = L.make_lp(3, 0)
+    assert lp.m == 479192 and lp.n == 1432800 and lp.name == "config3-seed0"
+    assert np.all(np.diff(lp.col_ptr) > 0)
