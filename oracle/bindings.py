@@ -16,6 +16,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_SO = os.path.join(HERE, "_build", "liboracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libhelp_ref.so")
 REF_BIN = os.path.join(HERE, "_ref", "help_ref")
+REF_LINDEP_BIN = os.path.join(HERE, "_ref", "help_ref_lindep")
 
 PIVOT_GREEDY = 0
 PIVOT_GIVEN = 1
@@ -73,6 +74,27 @@ def lib():
 
 def ref_available() -> bool:
     return os.path.exists(REF_SO)
+
+
+def ref_lindep_available() -> bool:
+    return os.path.exists(REF_LINDEP_BIN)
+
+
+def ref_lindep(mps_path: str, timeout: float = 600.0) -> dict:
+    """The reference's own dependent-row presolve (Presolve_Lindep.cpp with its
+    LUSOL, oracle/ref/ref_lindep.cpp) on one MPS file: {"rows", "dependent",
+    "status" (0 ok, 1 primal infeasible), "disabled"}, or {"error": ...} when
+    the reference program stops (LUSOL's fixed factor space runs out on
+    near-square random matrices: LUSOL_ANEEDMEM)."""
+    import json
+    import subprocess
+
+    r = subprocess.run([REF_LINDEP_BIN, mps_path], capture_output=True, text=True, timeout=timeout)
+    lines = [ln for ln in r.stdout.splitlines() if ln.startswith("{")]
+    if r.returncode != 0 or not lines:
+        tail = (r.stdout + r.stderr).strip().splitlines()
+        return {"error": "exit %d: %s" % (r.returncode, tail[-1] if tail else "")}
+    return json.loads(lines[-1])
 
 
 def ref():

@@ -3,7 +3,7 @@
  * MKL is not available on this machine, so each routine the reference's PCG
  * path calls is given its standard BLAS / sparse-BLAS meaning as a plain loop,
  * written from the BLAS definitions.  Used only to build the reference as a
- * test oracle.
+ * test oracle (its PCG path, and LUSOL under its dependent-row presolve).
  *
  * help_ref_nrm2_calls counts cblas_dnrm2 calls: ConjugateGradient calls it
  * once before its loop and once at the top of every pass (PCG.cpp:335, :341),
@@ -56,5 +56,25 @@ static inline void cblas_dscal(int n, double a, double* x, int incx) {
 }
 static inline void cblas_dcopy(int n, const double* x, int incx, double* y, int incy) {
     for (int i = 0; i < n; i++) y[i * incy] = x[i * incx];
+}
+/* The two further routines LUSOL's BLAS layer calls (lusol/myblas.cpp, used
+ * by the reference's dependent-row presolve). */
+static inline void cblas_dswap(int n, double* x, int incx, double* y, int incy) {
+    for (int i = 0; i < n; i++) {
+        const double t = x[i * incx];
+        x[i * incx] = y[i * incy];
+        y[i * incy] = t;
+    }
+}
+/* zero-based index of the first entry of largest magnitude (0 when n < 1) */
+static inline int cblas_idamax(int n, const double* x, int incx) {
+    int best = 0;
+    double vmax = -1.0;
+    for (int i = 0; i < n; i++)
+        if (fabs(x[i * incx]) > vmax) {
+            vmax = fabs(x[i * incx]);
+            best = i;
+        }
+    return best;
 }
 #endif
