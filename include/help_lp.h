@@ -91,15 +91,17 @@ int help_lp_read_bin(const char* path, help_lp* out);
 /* Linear-dependency presolve (the purpose of the reference's
  * Presolve_Lindep.cpp:316, off there by default, LP.h:72): *out gets in
  * without the rows that are linear combinations of the other rows, after
- * checking that b agrees to 1e-8 relative.  A row is dependent when sparse
- * elimination (Markowitz order, threshold pivoting) leaves none of its
- * entries above tol x its largest entry (the reference's TOLAPIV is 1e-8);
- * past a fill or work limit the last <= 4096 rows finish densely.  removed
- * (m flags, may be NULL) marks the dropped rows.  Returns the number of rows
- * dropped, -1 bad arguments, -2 out of memory, -3 b disagrees (the LP is
- * primal infeasible), -4 the presolve does not apply: elimination fills in
- * past 4 x nnz + 16 m entries or 64 x nnz + 2^28 entry updates with more
- * than 4096 rows left (random sparse A at 10^5 rows), *out left empty. */
+ * checking that b agrees to 1e-8 sqrt(1 + |b|_2^2).  A triangular crash
+ * peels the rows that have a column of their own; the rows it defers are
+ * reduced against the peeled ones and eliminated (Markowitz order, threshold
+ * pivoting, a dense finish for the last <= 4096 rows).  A row is dependent
+ * when none of its entries is left above tol x its largest entry (the
+ * reference's TOLAPIV is 1e-8).  removed (m flags, may be NULL) marks the
+ * dropped rows.  Returns the number of rows dropped, -1 bad arguments, -2 out
+ * of memory, -3 b disagrees (the LP is primal infeasible), -4 the presolve
+ * does not apply: the elimination fills in past its limits (4 x nnz + 16 m
+ * entries or 64 x nnz + 2^28 entry updates with more than 4096 rows left;
+ * random sparse A at 10^4 rows and more), *out left empty. */
 int help_lp_remove_dependent_rows(const help_lp* in, double tol, help_lp* out, int32_t* removed);
 
 /* Message of the last failed read on this thread ("" if none). */
