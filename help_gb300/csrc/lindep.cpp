@@ -323,7 +323,7 @@ RowMajor by_rows(const help_lp* in) {
 }
 
 // Triangular crash (the structure of Andersen's method, which the reference
-// follows: Presolve_Lindep.cpp:37-162): a row with a column no other
+// follows: Presolve_Lindep.cpp:34-167): a row with a column no other
 // remaining row holds is independent of the remaining rows -- it is peeled
 // with that column as its pivot; when no such column is left, the remaining
 // row with the most entries is deferred, which may free new columns.  The
