@@ -29,7 +29,7 @@ GENCODE = "-gencode=arch=compute_103a,code=sm_103a"
 GPU_CU = ["api.cu", "pcg.cu", "pcg_resident.cu", "renew.cu", "dense.cu", "vec.cu", "adat.cu", "noalloc.cu", "mlp.cu",
           "learned.cu", "mlp_api.cu"]
 GPU_CPP = ["items.cpp"]
-GPU_HDR = ["common.cuh", "spmv.cuh", "kernels.h", "context.h", "items.h", "mlp.h"]
+GPU_HDR = ["common.cuh", "spmv.cuh", "kernels.h", "context.h", "items.h", "mlp.h", "guard.h"]
 LP_CPP = ["lp_gen.cpp", "hsd.cpp", "lp_io.cpp", "lindep.cpp"]
 
 
@@ -79,7 +79,7 @@ def build_lp(verbose: bool = False) -> str:
     os.makedirs(LIBDIR, exist_ok=True)
     out = os.path.join(LIBDIR, "libhelp_lp.so")
     srcs = [os.path.join(CSRC, s) for s in LP_CPP]
-    deps = srcs + [os.path.join(ROOT, "include", "help_lp.h")]
+    deps = srcs + [os.path.join(ROOT, "include", "help_lp.h"), os.path.join(CSRC, "guard.h")]
     if _newer(out, deps):
         _run([CXX, "-O2", "-std=c++17", "-fPIC", "-shared", "-ffp-contract=off", "-Wall", "-o", out] + srcs)
     if verbose:

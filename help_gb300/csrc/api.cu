@@ -15,6 +15,7 @@
 #include <vector>
 
 #include "context.h"
+#include "guard.h"
 #include "mlp.h"
 #include "items.h"
 #include "kernels.h"
@@ -747,7 +748,7 @@ void help_pcg_default_options(help_pcg_options* o) {
     o->cg_path = 0;
 }
 
-int help_pcg_create(const help_pcg_options* opt, help_pcg** out) {
+static int help_pcg_create_body(const help_pcg_options* opt, help_pcg** out) {
     if (!out) return HELP_E_ARG;
     *out = nullptr;
     help_pcg* ctx = new (std::nothrow) help_pcg();
@@ -788,6 +789,10 @@ int help_pcg_create(const help_pcg_options* opt, help_pcg** out) {
     return HELP_OK;
 }
 
+int help_pcg_create(const help_pcg_options* opt, help_pcg** out) {
+    return c_guard(HELP_E_NOMEM, [&] { return help_pcg_create_body(opt, out); });
+}
+
 void help_pcg_free(help_pcg* ctx) {
     if (!ctx) return;
     cudaSetDevice(ctx->device);
@@ -803,7 +808,7 @@ void help_pcg_free(help_pcg* ctx) {
     delete ctx;
 }
 
-int help_pcg_construct(help_pcg* ctx, int32_t m, int32_t n, const int32_t* col_ptr, const int32_t* row_ind,
+static int help_pcg_construct_body(help_pcg* ctx, int32_t m, int32_t n, const int32_t* col_ptr, const int32_t* row_ind,
                        const double* val) {
     if (!ctx) return HELP_E_ARG;
     if (ctx->constructed) return fail(ctx, HELP_E_ARG, "construct: already constructed (call destruct first)");
@@ -881,7 +886,12 @@ int help_pcg_construct(help_pcg* ctx, int32_t m, int32_t n, const int32_t* col_p
     return HELP_OK;
 }
 
-int help_pcg_destruct(help_pcg* ctx) {
+int help_pcg_construct(help_pcg* ctx, int32_t m, int32_t n, const int32_t* col_ptr, const int32_t* row_ind,
+                       const double* val) {
+    return c_guard(HELP_E_NOMEM, [&] { return help_pcg_construct_body(ctx, m, n, col_ptr, row_ind, val); });
+}
+
+static int help_pcg_destruct_body(help_pcg* ctx) {
     if (!ctx) return HELP_E_ARG;
     cudaSetDevice(ctx->device);
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
@@ -894,7 +904,11 @@ int help_pcg_destruct(help_pcg* ctx) {
     return HELP_OK;
 }
 
-int help_pcg_renew(help_pcg* ctx, const double* d) {
+int help_pcg_destruct(help_pcg* ctx) {
+    return c_guard(HELP_E_NOMEM, [&] { return help_pcg_destruct_body(ctx); });
+}
+
+static int help_pcg_renew_body(help_pcg* ctx, const double* d) {
     if (!ctx || !d) return HELP_E_ARG;
     if (!ctx->constructed) return fail(ctx, HELP_E_ARG, "renew: construct first");
     CK(cudaSetDevice(ctx->device));
@@ -907,7 +921,11 @@ int help_pcg_renew(help_pcg* ctx, const double* d) {
     return HELP_OK;
 }
 
-int help_pcg_solve(help_pcg* ctx, const double* d, const double* b_1, const double* b_2, double* x_1,
+int help_pcg_renew(help_pcg* ctx, const double* d) {
+    return c_guard(HELP_E_NOMEM, [&] { return help_pcg_renew_body(ctx, d); });
+}
+
+static int help_pcg_solve_body(help_pcg* ctx, const double* d, const double* b_1, const double* b_2, double* x_1,
                    double* x_2) {
     if (!ctx || !d || !b_1 || !b_2 || !x_1 || !x_2) return HELP_E_ARG;
     if (!ctx->constructed) return fail(ctx, HELP_E_ARG, "solve: construct first");
@@ -1001,6 +1019,11 @@ int help_pcg_solve(help_pcg* ctx, const double* d, const double* b_1, const doub
     return HELP_OK;
 }
 
+int help_pcg_solve(help_pcg* ctx, const double* d, const double* b_1, const double* b_2, double* x_1,
+                   double* x_2) {
+    return c_guard(HELP_E_NOMEM, [&] { return help_pcg_solve_body(ctx, d, b_1, b_2, x_1, x_2); });
+}
+
 int help_pcg_get_stats(const help_pcg* ctx, help_pcg_stats* out) {
     if (!ctx || !out) return HELP_E_ARG;
     *out = ctx->stats;
@@ -1009,7 +1032,7 @@ int help_pcg_get_stats(const help_pcg* ctx, help_pcg_stats* out) {
 
 const char* help_pcg_last_error(const help_pcg* ctx) { return ctx ? ctx->err.c_str() : "null context"; }
 
-int help_pcg_matvec_dev(help_pcg* ctx, int32_t op, int32_t fp32, const void* x, void* y, void* stream) {
+static int help_pcg_matvec_dev_body(help_pcg* ctx, int32_t op, int32_t fp32, const void* x, void* y, void* stream) {
     if (!ctx || !x || !y) return HELP_E_ARG;
     if (!ctx->constructed) return fail(ctx, HELP_E_ARG, "matvec: construct first");
     if ((op >= HELP_OP_ADAT || fp32) && !ctx->renewed) return fail(ctx, HELP_E_ARG, "matvec: renew first");
@@ -1056,7 +1079,11 @@ int help_pcg_matvec_dev(help_pcg* ctx, int32_t op, int32_t fp32, const void* x, 
     return HELP_OK;
 }
 
-int help_pcg_matvec(help_pcg* ctx, int32_t op, const double* x, double* y) {
+int help_pcg_matvec_dev(help_pcg* ctx, int32_t op, int32_t fp32, const void* x, void* y, void* stream) {
+    return c_guard(HELP_E_NOMEM, [&] { return help_pcg_matvec_dev_body(ctx, op, fp32, x, y, stream); });
+}
+
+static int help_pcg_matvec_body(help_pcg* ctx, int32_t op, const double* x, double* y) {
     if (!ctx || !x || !y) return HELP_E_ARG;
     if (!ctx->constructed) return fail(ctx, HELP_E_ARG, "matvec: construct first");
     CK(cudaSetDevice(ctx->device));
@@ -1077,7 +1104,11 @@ int help_pcg_matvec(help_pcg* ctx, int32_t op, const double* x, double* y) {
     return d2h(ctx, y, ctx->res.as<double>(), nout);
 }
 
-int help_pcg_matvec_acc(help_pcg* ctx, int32_t transpose, int32_t sign, const double* v, double* dest) {
+int help_pcg_matvec(help_pcg* ctx, int32_t op, const double* x, double* y) {
+    return c_guard(HELP_E_NOMEM, [&] { return help_pcg_matvec_body(ctx, op, x, y); });
+}
+
+static int help_pcg_matvec_acc_body(help_pcg* ctx, int32_t transpose, int32_t sign, const double* v, double* dest) {
     if (!ctx || !v || !dest || (sign != 1 && sign != -1)) return HELP_E_ARG;
     if (!ctx->constructed) return fail(ctx, HELP_E_ARG, "matvec: construct first");
     CK(cudaSetDevice(ctx->device));
@@ -1103,7 +1134,11 @@ int help_pcg_matvec_acc(help_pcg* ctx, int32_t transpose, int32_t sign, const do
     return d2h(ctx, dest, ctx->x2.as<double>(), nout);
 }
 
-int help_pcg_precond_apply(help_pcg* ctx, const double* r, double* z) {
+int help_pcg_matvec_acc(help_pcg* ctx, int32_t transpose, int32_t sign, const double* v, double* dest) {
+    return c_guard(HELP_E_NOMEM, [&] { return help_pcg_matvec_acc_body(ctx, transpose, sign, v, dest); });
+}
+
+static int help_pcg_precond_apply_body(help_pcg* ctx, const double* r, double* z) {
     if (!ctx || !r || !z) return HELP_E_ARG;
     if (!ctx->renewed) return fail(ctx, HELP_E_ARG, "precond: renew first");
     CK(cudaSetDevice(ctx->device));
@@ -1117,7 +1152,11 @@ int help_pcg_precond_apply(help_pcg* ctx, const double* r, double* z) {
     return d2h(ctx, z, ctx->p1.as<double>(), ctx->m);
 }
 
-int help_pcg_get_pivots(help_pcg* ctx, int32_t* pivots, double* diag_g, double* diag_s) {
+int help_pcg_precond_apply(help_pcg* ctx, const double* r, double* z) {
+    return c_guard(HELP_E_NOMEM, [&] { return help_pcg_precond_apply_body(ctx, r, z); });
+}
+
+static int help_pcg_get_pivots_body(help_pcg* ctx, int32_t* pivots, double* diag_g, double* diag_s) {
     if (!ctx) return HELP_E_ARG;
     if (!ctx->renewed) return fail(ctx, HELP_E_ARG, "pivots: renew first");
     CK(cudaSetDevice(ctx->device));
@@ -1134,7 +1173,11 @@ int help_pcg_get_pivots(help_pcg* ctx, int32_t* pivots, double* diag_g, double* 
     return rc;
 }
 
-int help_pcg_cg(help_pcg* ctx, const double* b, double* x, int64_t* iters) {
+int help_pcg_get_pivots(help_pcg* ctx, int32_t* pivots, double* diag_g, double* diag_s) {
+    return c_guard(HELP_E_NOMEM, [&] { return help_pcg_get_pivots_body(ctx, pivots, diag_g, diag_s); });
+}
+
+static int help_pcg_cg_body(help_pcg* ctx, const double* b, double* x, int64_t* iters) {
     if (!ctx || !b || !x) return HELP_E_ARG;
     if (!ctx->renewed) return fail(ctx, HELP_E_ARG, "cg: renew first");
     CK(cudaSetDevice(ctx->device));
@@ -1154,7 +1197,11 @@ int help_pcg_cg(help_pcg* ctx, const double* b, double* x, int64_t* iters) {
     return d2h(ctx, x, ctx->x.as<double>(), ctx->m);
 }
 
-int help_pcg_cg_f32(help_pcg* ctx, const double* b, double* x, int64_t* iters) {
+int help_pcg_cg(help_pcg* ctx, const double* b, double* x, int64_t* iters) {
+    return c_guard(HELP_E_NOMEM, [&] { return help_pcg_cg_body(ctx, b, x, iters); });
+}
+
+static int help_pcg_cg_f32_body(help_pcg* ctx, const double* b, double* x, int64_t* iters) {
     if (!ctx || !b || !x) return HELP_E_ARG;
     if (!ctx->renewed) return fail(ctx, HELP_E_ARG, "cg_f32: renew first");
     if (ctx->opt.precision != HELP_PREC_MIXED)
@@ -1181,7 +1228,11 @@ int help_pcg_cg_f32(help_pcg* ctx, const double* b, double* x, int64_t* iters) {
     return d2h(ctx, x, ctx->x.as<double>(), m);
 }
 
-int help_pcg_attach_mlp(help_pcg* ctx, help_mlp* mlp) {
+int help_pcg_cg_f32(help_pcg* ctx, const double* b, double* x, int64_t* iters) {
+    return c_guard(HELP_E_NOMEM, [&] { return help_pcg_cg_f32_body(ctx, b, x, iters); });
+}
+
+static int help_pcg_attach_mlp_body(help_pcg* ctx, help_mlp* mlp) {
     if (!ctx) return HELP_E_ARG;
     if (mlp && help_mlp_device(mlp) != ctx->device)
         return fail(ctx, HELP_E_ARG, "attach_mlp: the model lives on another device");
@@ -1195,7 +1246,11 @@ int help_pcg_attach_mlp(help_pcg* ctx, help_mlp* mlp) {
     return HELP_OK;
 }
 
-int help_pcg_features(help_pcg* ctx, int32_t slot, float* x) {
+int help_pcg_attach_mlp(help_pcg* ctx, help_mlp* mlp) {
+    return c_guard(HELP_E_NOMEM, [&] { return help_pcg_attach_mlp_body(ctx, mlp); });
+}
+
+static int help_pcg_features_body(help_pcg* ctx, int32_t slot, float* x) {
     if (!ctx || !x || slot < 0 || slot >= kSolveSlots) return HELP_E_ARG;
     if (!ctx->renewed) return fail(ctx, HELP_E_ARG, "features: renew first");
     CK(cudaSetDevice(ctx->device));
@@ -1205,7 +1260,11 @@ int help_pcg_features(help_pcg* ctx, int32_t slot, float* x) {
     return HELP_OK;
 }
 
-int help_adat_assemble(help_pcg* ctx, const double* w, int32_t* row_ptr, int32_t* col, double* val, int64_t* nnz) {
+int help_pcg_features(help_pcg* ctx, int32_t slot, float* x) {
+    return c_guard(HELP_E_NOMEM, [&] { return help_pcg_features_body(ctx, slot, x); });
+}
+
+static int help_adat_assemble_body(help_pcg* ctx, const double* w, int32_t* row_ptr, int32_t* col, double* val, int64_t* nnz) {
     if (!ctx || !w || !row_ptr || !nnz) return HELP_E_ARG;
     if (!ctx->constructed) return fail(ctx, HELP_E_ARG, "adat: construct first");
     CK(cudaSetDevice(ctx->device));
@@ -1238,6 +1297,10 @@ int help_adat_assemble(help_pcg* ctx, const double* w, int32_t* row_ptr, int32_t
     CK(cudaMemcpyAsync(val, dv, 8 * (size_t)total, cudaMemcpyDeviceToHost, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
     return HELP_OK;
+}
+
+int help_adat_assemble(help_pcg* ctx, const double* w, int32_t* row_ptr, int32_t* col, double* val, int64_t* nnz) {
+    return c_guard(HELP_E_NOMEM, [&] { return help_adat_assemble_body(ctx, w, row_ptr, col, val, nnz); });
 }
 
 }  // extern "C"

@@ -21,6 +21,7 @@
 #include <vector>
 
 #include "../../include/help_lp.h"
+#include "guard.h"
 
 namespace {
 
@@ -461,8 +462,8 @@ void help_hsd_default_options(help_hsd_options* o) {
     o->dinf_tol = 1e-8;
 }
 
-int help_hsd_solve(const help_lp* lp, const help_ne_backend* be, const help_hsd_options* opt_in,
-                   help_hsd_result* res, double* x_out, double* y_out) {
+static int hsd_solve(const help_lp* lp, const help_ne_backend* be, const help_hsd_options* opt_in,
+                     help_hsd_result* res, double* x_out, double* y_out) {
     if (!lp || !be || !res || !be->construct || !be->renew || !be->solve || !be->destruct) return -1;
     help_hsd_options dflt;
     help_hsd_default_options(&dflt);
@@ -508,6 +509,11 @@ int help_hsd_solve(const help_lp* lp, const help_ne_backend* be, const help_hsd_
     if (y_out)
         for (size_t i = 0; i < m; ++i) y_out[i] = h.y[i] / h.tau;
     return h.be_error ? -2 : 0;
+}
+
+int help_hsd_solve(const help_lp* lp, const help_ne_backend* be, const help_hsd_options* opt_in,
+                   help_hsd_result* res, double* x_out, double* y_out) {
+    return c_guard(-3, [&] { return hsd_solve(lp, be, opt_in, res, x_out, y_out); });
 }
 
 }  // extern "C"

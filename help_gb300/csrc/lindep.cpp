@@ -43,6 +43,7 @@
 #include <vector>
 
 #include "../../include/help_lp.h"
+#include "guard.h"
 
 namespace {
 
@@ -557,13 +558,7 @@ int eliminate(Lindep& S, double tol, int64_t fill_limit, int64_t work_limit) {
     return 0;
 }
 
-}  // namespace
-
-extern "C" {
-
-int help_lp_remove_dependent_rows(const help_lp* in, double tol, help_lp* out, int32_t* removed) {
-    if (!in || !out || in->m <= 0 || in->n <= 0 || !(tol > 0.0)) return -1;
-    std::memset(out, 0, sizeof(*out));
+int remove_dependent_rows(const help_lp* in, double tol, help_lp* out, int32_t* removed) {
     const int32_t m = in->m, n = in->n;
     const int64_t nnz = in->nnz;
     std::vector<double> row_scale((size_t)m, 0.0);  // largest |entry| of each row
@@ -662,6 +657,18 @@ int help_lp_remove_dependent_rows(const help_lp* in, double tol, help_lp* out, i
     if (removed)
         for (int32_t i = 0; i < m; ++i) removed[i] = dep[i];
     return n_dep;
+}
+
+}  // namespace
+
+extern "C" {
+
+int help_lp_remove_dependent_rows(const help_lp* in, double tol, help_lp* out, int32_t* removed) {
+    if (!in || !out || in->m <= 0 || in->n <= 0 || !(tol > 0.0)) return -1;
+    std::memset(out, 0, sizeof(*out));
+    const int rc = c_guard(-2, [&] { return remove_dependent_rows(in, tol, out, removed); });
+    if (rc == -2) help_lp_free(out);
+    return rc;
 }
 
 }  // extern "C"

@@ -16,6 +16,7 @@
 // rounded value of the same decimal.
 
 #include "../../include/help_lp.h"
+#include "guard.h"
 
 #include <algorithm>
 #include <cmath>
@@ -498,13 +499,17 @@ extern "C" {
 int help_lp_generate(const help_lp_spec* spec, uint64_t seed, help_lp* out) {
     if (!spec || !out) return -1;
     std::memset(out, 0, sizeof(*out));
-    switch (spec->kind) {
-        case HELP_LP_RANDOM: return gen_random(spec, seed, out);
-        case HELP_LP_ZIPF: return gen_zipf(spec, seed, out);
-        case HELP_LP_MCF: return gen_mcf(spec, seed, out);
-        case HELP_LP_BLOCK: return gen_block(spec, seed, out);
-        default: return -1;
-    }
+    const int rc = c_guard(-2, [&] {
+        switch (spec->kind) {
+            case HELP_LP_RANDOM: return gen_random(spec, seed, out);
+            case HELP_LP_ZIPF: return gen_zipf(spec, seed, out);
+            case HELP_LP_MCF: return gen_mcf(spec, seed, out);
+            case HELP_LP_BLOCK: return gen_block(spec, seed, out);
+            default: return -1;
+        }
+    });
+    if (rc < -1) help_lp_free(out);  // allocation failed part way
+    return rc;
 }
 
 void help_lp_free(help_lp* lp) {
@@ -542,18 +547,20 @@ int help_lp_write_mps(const help_lp* lp, const char* path) {
 int help_csc_to_csr(int32_t m, int32_t n, const int32_t* col_ptr, const int32_t* row_ind,
                     const double* val, int32_t* row_ptr, int32_t* col_ind, double* val_out) {
     if (m < 0 || n < 0) return -1;
-    for (int32_t i = 0; i <= m; ++i) row_ptr[i] = 0;
-    const int32_t nnz = col_ptr[n];
-    for (int32_t p = 0; p < nnz; ++p) row_ptr[row_ind[p] + 1]++;
-    for (int32_t i = 0; i < m; ++i) row_ptr[i + 1] += row_ptr[i];
-    std::vector<int32_t> fill(row_ptr, row_ptr + m);
-    for (int32_t j = 0; j < n; ++j)
-        for (int32_t p = col_ptr[j]; p < col_ptr[j + 1]; ++p) {
-            const int32_t q = fill[row_ind[p]]++;
-            col_ind[q] = j;
-            if (val_out) val_out[q] = val[p];
-        }
-    return 0;
+    return c_guard(-2, [&] {
+        for (int32_t i = 0; i <= m; ++i) row_ptr[i] = 0;
+        const int32_t nnz = col_ptr[n];
+        for (int32_t p = 0; p < nnz; ++p) row_ptr[row_ind[p] + 1]++;
+        for (int32_t i = 0; i < m; ++i) row_ptr[i + 1] += row_ptr[i];
+        std::vector<int32_t> fill(row_ptr, row_ptr + m);
+        for (int32_t j = 0; j < n; ++j)
+            for (int32_t p = col_ptr[j]; p < col_ptr[j + 1]; ++p) {
+                const int32_t q = fill[row_ind[p]]++;
+                col_ind[q] = j;
+                if (val_out) val_out[q] = val[p];
+            }
+        return 0;
+    });
 }
 
 }  // extern "C"

@@ -22,6 +22,7 @@
 #include <algorithm>
 
 #include "../../include/help_lp.h"
+#include "guard.h"
 
 namespace {
 
@@ -89,18 +90,10 @@ struct Column {
     std::vector<std::pair<int32_t, double>> entries;
 };
 
-}  // namespace
-
-extern "C" {
-
-const char* help_lp_last_error(void) { return g_err.c_str(); }
-
-int help_lp_read_mps(const char* path, help_lp* out) {
-    g_err.clear();
-    if (!path || !out) return fail(-1, "bad arguments");
-    std::memset(out, 0, sizeof(*out));
-    FILE* f = std::fopen(path, "r");
-    if (!f) return fail(-2, std::string("cannot open ") + path);
+int read_mps_impl(const char* path, help_lp* out) {
+    ScopedFile file(std::fopen(path, "r"));
+    if (!file.f) return fail(-2, std::string("cannot open ") + path);
+    FILE* f = file.f;
     std::unordered_map<std::string, int32_t> row_id, col_id;
     std::vector<char> row_type;
     std::vector<double> rhs;
@@ -109,10 +102,7 @@ int help_lp_read_mps(const char* path, help_lp* out) {
     std::vector<std::string> tok;
     enum { kNone, kRows, kColumns, kRhs, kBounds, kDone } sec = kNone;
     long long lineno = 0;
-    auto err = [&](const std::string& why) {
-        std::fclose(f);
-        return fail(-3, "line " + std::to_string(lineno) + ": " + why);
-    };
+    auto err = [&](const std::string& why) { return fail(-3, "line " + std::to_string(lineno) + ": " + why); };
     while (read_line(f, line)) {
         ++lineno;
         if (line.empty() || line[0] == '*') continue;
@@ -199,7 +189,7 @@ int help_lp_read_mps(const char* path, help_lp* out) {
                 return err("data line outside a section");
         }
     }
-    std::fclose(f);
+    file.close();
     if (sec != kDone) return fail(-3, "missing ENDATA");
     if (obj_name.empty()) return fail(-3, "no objective (N) row");
     const int32_t m = (int32_t)row_type.size();
@@ -244,6 +234,22 @@ int help_lp_read_mps(const char* path, help_lp* out) {
     }
     out->col_ptr[n] = (int32_t)p;
     return 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* help_lp_last_error(void) { return g_err.c_str(); }
+
+int help_lp_read_mps(const char* path, help_lp* out) {
+    g_err.clear();
+    if (!path || !out) return fail(-1, "bad arguments");
+    std::memset(out, 0, sizeof(*out));
+    const int rc = c_guard(-4, [&] { return read_mps_impl(path, out); });
+    if (rc != -4) return rc;
+    help_lp_free(out);
+    return fail(-2, "out of memory");
 }
 
 int help_lp_write_bin(const help_lp* lp, const char* path) {

@@ -10,6 +10,7 @@
 
 #include "../../include/help_gpu.h"
 #include "context.h"
+#include "guard.h"
 #include "mlp.h"
 
 struct help_mlp {
@@ -72,7 +73,7 @@ int loss_grad(help_mlp* mlp, const void* x, const float* t, const float* wt, lon
 
 extern "C" {
 
-int help_mlp_create(int32_t device, help_mlp** out) {
+static int help_mlp_create_body(int32_t device, help_mlp** out) {
     if (!out) return HELP_E_ARG;
     *out = nullptr;
     help_mlp* mlp = new help_mlp();
@@ -96,7 +97,11 @@ int help_mlp_create(int32_t device, help_mlp** out) {
     return HELP_OK;
 }
 
-int help_mlp_free(help_mlp* mlp) {
+int help_mlp_create(int32_t device, help_mlp** out) {
+    return c_guard(HELP_E_NOMEM, [&] { return help_mlp_create_body(device, out); });
+}
+
+static int help_mlp_free_body(help_mlp* mlp) {
     if (!mlp) return HELP_E_ARG;
     cudaSetDevice(mlp->device);
     for (help::DevMem* d : {&mlp->prm, &mlp->m1, &mlp->m2, &mlp->grad, &mlp->w, &mlp->out, &mlp->g3, &mlp->h1,
@@ -107,9 +112,13 @@ int help_mlp_free(help_mlp* mlp) {
     return HELP_OK;
 }
 
+int help_mlp_free(help_mlp* mlp) {
+    return c_guard(HELP_E_NOMEM, [&] { return help_mlp_free_body(mlp); });
+}
+
 const char* help_mlp_last_error(const help_mlp* mlp) { return mlp ? mlp->err.c_str() : "null model"; }
 
-int help_mlp_set_params(help_mlp* mlp, const float* params) {
+static int help_mlp_set_params_body(help_mlp* mlp, const float* params) {
     if (!mlp || !params) return HELP_E_ARG;
     for (int j = 0; j < HELP_MLP_PARAMS; ++j)
         if (!std::isfinite(params[j])) return mfail(mlp, HELP_E_NUMERIC, "mlp: non-finite parameter");
@@ -123,7 +132,11 @@ int help_mlp_set_params(help_mlp* mlp, const float* params) {
     return HELP_OK;
 }
 
-int help_mlp_get_params(help_mlp* mlp, float* params) {
+int help_mlp_set_params(help_mlp* mlp, const float* params) {
+    return c_guard(HELP_E_NOMEM, [&] { return help_mlp_set_params_body(mlp, params); });
+}
+
+static int help_mlp_get_params_body(help_mlp* mlp, float* params) {
     if (!mlp || !params) return HELP_E_ARG;
     MCK(cudaSetDevice(mlp->device));
     MCK(cudaMemcpyAsync(params, mlp->prm.p, sizeof(float) * HELP_MLP_PARAMS, cudaMemcpyDeviceToHost, mlp->stream));
@@ -131,7 +144,11 @@ int help_mlp_get_params(help_mlp* mlp, float* params) {
     return HELP_OK;
 }
 
-int help_mlp_forward(help_mlp* mlp, const void* x, int64_t rows, float* out, void* stream) {
+int help_mlp_get_params(help_mlp* mlp, float* params) {
+    return c_guard(HELP_E_NOMEM, [&] { return help_mlp_get_params_body(mlp, params); });
+}
+
+static int help_mlp_forward_body(help_mlp* mlp, const void* x, int64_t rows, float* out, void* stream) {
     if (!mlp || !x || !out || rows < 0) return HELP_E_ARG;
     MCK(cudaSetDevice(mlp->device));
     MCK(help::mlp_forward(static_cast<const __nv_bfloat16*>(x), rows, mlp->w.as<help::MlpDevWeights>(), out, nullptr,
@@ -139,7 +156,11 @@ int help_mlp_forward(help_mlp* mlp, const void* x, int64_t rows, float* out, voi
     return HELP_OK;
 }
 
-int help_mlp_loss_grad(help_mlp* mlp, const void* x, const float* target, const float* weight, int64_t rows,
+int help_mlp_forward(help_mlp* mlp, const void* x, int64_t rows, float* out, void* stream) {
+    return c_guard(HELP_E_NOMEM, [&] { return help_mlp_forward_body(mlp, x, rows, out, stream); });
+}
+
+static int help_mlp_loss_grad_body(help_mlp* mlp, const void* x, const float* target, const float* weight, int64_t rows,
                        double* loss, float* grad) {
     if (!mlp) return HELP_E_ARG;
     MCK(cudaSetDevice(mlp->device));
@@ -153,7 +174,12 @@ int help_mlp_loss_grad(help_mlp* mlp, const void* x, const float* target, const 
     return HELP_OK;
 }
 
-int help_mlp_train_step(help_mlp* mlp, const void* x, const float* target, const float* weight, int64_t rows,
+int help_mlp_loss_grad(help_mlp* mlp, const void* x, const float* target, const float* weight, int64_t rows,
+                       double* loss, float* grad) {
+    return c_guard(HELP_E_NOMEM, [&] { return help_mlp_loss_grad_body(mlp, x, target, weight, rows, loss, grad); });
+}
+
+static int help_mlp_train_step_body(help_mlp* mlp, const void* x, const float* target, const float* weight, int64_t rows,
                         float lr, double* loss) {
     if (!mlp || !(lr > 0.f)) return HELP_E_ARG;
     MCK(cudaSetDevice(mlp->device));
@@ -164,6 +190,11 @@ int help_mlp_train_step(help_mlp* mlp, const void* x, const float* target, const
                        mlp->step, mlp->w.as<help::MlpDevWeights>(), mlp->stream));
     MCK(cudaStreamSynchronize(mlp->stream));
     return HELP_OK;
+}
+
+int help_mlp_train_step(help_mlp* mlp, const void* x, const float* target, const float* weight, int64_t rows,
+                        float lr, double* loss) {
+    return c_guard(HELP_E_NOMEM, [&] { return help_mlp_train_step_body(mlp, x, target, weight, rows, lr, loss); });
 }
 
 }  // extern "C"

@@ -77,8 +77,8 @@ int help_lp_write_mps(const help_lp* lp, const char* path);
  * entries below 1e-8 in magnitude are dropped (MPSRead.cpp:148-163); rows are
  * sorted inside each column and a repeated (row, column) entry is an error.
  * RANGES and every bound other than x >= 0 (LO 0, PL) are rejected, as are
- * integer markers.  Returns 0, -1 bad arguments, -2 I/O error, -3 format
- * error (help_lp_last_error() tells which line and why). */
+ * integer markers.  Returns 0, -1 bad arguments, -2 I/O error or out of
+ * memory, -3 format error (help_lp_last_error() tells which line and why). */
 int help_lp_read_mps(const char* path, help_lp* out);
 
 /* Binary fast path for large instances (no text parsing): a 64-byte header
@@ -166,7 +166,10 @@ typedef struct help_hsd_result {
 void help_hsd_default_options(help_hsd_options* opt);
 
 /* Runs the HSD method (the reference's HSD_Main, HSDSolver.cpp:869-883) on an
- * all-lower-bounded standard-form LP.  x_out (n) / y_out (m) may be NULL. */
+ * all-lower-bounded standard-form LP.  x_out (n) / y_out (m) may be NULL.
+ * Returns 0, -1 bad arguments, the backend's construct code when that
+ * fails, -2 when a later backend call failed, -3 host out of memory (the
+ * backend may then still hold its construct). */
 int help_hsd_solve(const help_lp* lp, const help_ne_backend* be, const help_hsd_options* opt,
                    help_hsd_result* res, double* x_out, double* y_out);
 
