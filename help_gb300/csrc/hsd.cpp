@@ -511,9 +511,42 @@ static int hsd_solve(const help_lp* lp, const help_ne_backend* be, const help_hs
     return h.be_error ? -2 : 0;
 }
 
+// With presolve_lindep: the dependent rows removed first, the reduced LP
+// solved, y scattered back with 0 on the dropped rows (a dropped row is a
+// combination of kept ones, so A^T y and b^T y are unchanged).
+static int hsd_solve_presolved(const help_lp* lp, const help_ne_backend* be, const help_hsd_options* opt,
+                               help_hsd_result* res, double* x_out, double* y_out) {
+    if (!lp || !be || !res || lp->m <= 0 || lp->n <= 0) return hsd_solve(lp, be, opt, res, x_out, y_out);
+    help_lp red;
+    std::vector<int32_t> removed((size_t)lp->m, 0);
+    const int rc = help_lp_remove_dependent_rows(lp, 1e-8, &red, removed.data());
+    if (rc == -3) {  // b disagrees with a dependency: primal infeasible, no HSD run
+        std::memset(res, 0, sizeof(*res));
+        res->lp_status = 1;
+        return 0;
+    }
+    if (rc <= 0) {  // nothing removed, or the presolve does not apply
+        help_lp_free(&red);
+        if (rc == -2) return -3;
+        return hsd_solve(lp, be, opt, res, x_out, y_out);
+    }
+    std::vector<double> y_red(y_out ? (size_t)red.m : 0);
+    const int r = hsd_solve(&red, be, opt, res, x_out, y_out ? y_red.data() : nullptr);
+    help_lp_free(&red);
+    if (y_out) {
+        size_t k = 0;
+        for (int32_t i = 0; i < lp->m; ++i) y_out[i] = removed[(size_t)i] ? 0.0 : y_red[k++];
+    }
+    res->rows_removed = rc;
+    return r;
+}
+
 int help_hsd_solve(const help_lp* lp, const help_ne_backend* be, const help_hsd_options* opt_in,
                    help_hsd_result* res, double* x_out, double* y_out) {
-    return c_guard(-3, [&] { return hsd_solve(lp, be, opt_in, res, x_out, y_out); });
+    return c_guard(-3, [&] {
+        if (opt_in && opt_in->presolve_lindep) return hsd_solve_presolved(lp, be, opt_in, res, x_out, y_out);
+        return hsd_solve(lp, be, opt_in, res, x_out, y_out);
+    });
 }
 
 }  // extern "C"

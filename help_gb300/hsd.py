@@ -9,11 +9,14 @@ from . import native
 
 
 def solve_lp(lp, backend: native.NeBackend, *, verbose: bool = False, max_iterations: int = 10000,
-             gap_tol: float = 1e-8, on_iter=None, want_solution: bool = False) -> dict:
+             gap_tol: float = 1e-8, on_iter=None, want_solution: bool = False,
+             presolve_lindep: bool = False) -> dict:
     """Run HSD_Main (HSDSolver.cpp:869-883) on ``lp`` with ``backend``'s four entry points.
 
     Returns a dict with status, iterations, objective values, gap, infeasibilities,
-    total and backend wall time (and x, y when ``want_solution``).
+    total and backend wall time, lp_status / rows_removed of the dependent-row
+    presolve (``presolve_lindep``: the reference's PRESOLVE_LINDEP switch,
+    LP.h:72), and x, y when ``want_solution``.
     """
     lib = native.lp_lib()
     opt = native.HsdOptions()
@@ -21,6 +24,7 @@ def solve_lp(lp, backend: native.NeBackend, *, verbose: bool = False, max_iterat
     opt.max_iterations = max_iterations
     opt.gap_tol = gap_tol
     opt.verbose = int(verbose)
+    opt.presolve_lindep = int(presolve_lindep)
     cb = None
     if on_iter is not None:
         def _cb(user, it, s6):

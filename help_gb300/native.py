@@ -151,6 +151,7 @@ class HsdOptions(C.Structure):
         ("verbose", C.c_int32),
         ("on_iter", C.c_void_p),
         ("user", C.c_void_p),
+        ("presolve_lindep", C.c_int32),
     ]
 
 
@@ -169,6 +170,8 @@ class HsdResult(C.Structure):
         ("kappa", C.c_double),
         ("wall_s", C.c_double),
         ("backend_s", C.c_double),
+        ("lp_status", C.c_int32),
+        ("rows_removed", C.c_int32),
     ]
 
 

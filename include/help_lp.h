@@ -151,6 +151,12 @@ typedef struct help_hsd_options {
      * primal infeasibility, dual infeasibility); may be NULL. */
     void (*on_iter)(void* user, int32_t iter, const double* stats6);
     void* user;
+    /* Remove the dependent rows first (help_lp_remove_dependent_rows, tol
+     * 1e-8), as the reference does when PRESOLVE_LINDEP is set (LP.h:72, 0
+     * there; Presolve.cpp:1254-1260): the backend then sees the reduced
+     * matrix, y_out still has m entries (0 on the dropped rows).  Where the
+     * presolve does not apply (its -4) the LP is solved as it is. */
+    int32_t presolve_lindep;
 } help_hsd_options;
 
 typedef struct help_hsd_result {
@@ -161,6 +167,10 @@ typedef struct help_hsd_result {
     double primal_obj, dual_obj, rel_gap, primal_infeas, dual_infeas;
     double tau, kappa;
     double wall_s, backend_s;   /* total and time spent inside backend calls     */
+    int32_t lp_status;          /* 0 OK, 1 primal infeasible found by the presolve
+                                   (the reference's LP_Status, LP.h:77-80; no
+                                   HSD iteration is run then)                   */
+    int32_t rows_removed;       /* dependent rows the presolve dropped           */
 } help_hsd_result;
 
 void help_hsd_default_options(help_hsd_options* opt);

@@ -205,3 +205,35 @@ def test_config3_generated_full_then_presolved():
     lp = L.make_lp(3, 0)
     assert lp.m == 479192 and lp.n == 1432800 and lp.name == "config3-seed0"
     assert np.all(np.diff(lp.col_ptr) > 0)
+
+
+def test_hsd_driver_presolve_switch():
+    """help_hsd_options.presolve_lindep (the reference's PRESOLVE_LINDEP): the
+    driver removes the dependent rows itself, reaches the grounded optimum,
+    reports how many rows went, and returns y for all m rows (0 on the
+    dropped ones) -- b^T y over the full rows equals the objective; with b
+    moved along a dependency it reports primal infeasibility and runs no
+    iteration."""
+    from help_gb300 import hsd
+    from oracle import bindings as ob
+
+    def backend():
+        return ob.OracleNormalEquations(pivots=10, tol=1e-14, max_iter=10**6).ne_backend()
+
+    full = L.generate(L.spec_mcf(8, 3, 2, grounded=False), 4)
+    grounded = L.generate(L.spec_mcf(8, 3, 2), 4)
+    r = hsd.solve_lp(full, backend(), presolve_lindep=True, want_solution=True)
+    g = hsd.solve_lp(grounded, backend())
+    assert r["rc"] == 0 and r["status"] == 0 and r["lp_status"] == 0 and r["rows_removed"] == 3
+    assert abs(r["primal_obj"] - g["primal_obj"]) <= 1e-7 * (1 + abs(g["primal_obj"]))
+    assert len(r["y"]) == full.m and np.count_nonzero(r["y"] == 0.0) >= 3
+    assert abs(full.b @ r["y"] - r["primal_obj"]) <= 1e-6 * (1 + abs(r["primal_obj"]))
+    assert np.linalg.norm(dense(full) @ r["x"] - full.b) <= 1e-7 * (1 + np.linalg.norm(full.b))
+    bad = L.generate(L.spec_mcf(8, 3, 2, grounded=False), 4)
+    bad.b = bad.b.copy()
+    bad.b[70] += 0.5
+    r = hsd.solve_lp(bad, backend(), presolve_lindep=True)
+    assert r["rc"] == 0 and r["lp_status"] == 1 and r["iterations"] == 0
+    # on a full-rank LP the switch leaves the run as it is
+    r0 = hsd.solve_lp(grounded, backend(), presolve_lindep=True)
+    assert r0["rows_removed"] == 0 and r0["iterations"] == g["iterations"] and r0["primal_obj"] == g["primal_obj"]
