@@ -406,7 +406,7 @@ int normal_solve(help_pcg* ctx, const double* rhs, double* x, bool warm, long lo
         prev = rr;
     }
     *outer_out = outer;
-    if (!ok && ctx->opt.fallback) {
+    if (!ok && ctx->opt.fallback) {  // the mixed form's FP64 finish
         CgResult res;
         const double tol = (rr > 0.0) ? ctx->opt.ir_tol * std::sqrt(rhs2 / rr) : 1.0;
         rc = run_pcg<double>(ctx, x, r, std::min(tol, 1.0), ctx->opt.cg_max_iter, 0, &res);
@@ -746,6 +746,7 @@ void help_pcg_default_options(help_pcg_options* o) {
     o->warm_start = 0;
     o->fallback = 1;
     o->cg_path = 0;
+    o->cap_ok = 0;
 }
 
 static int help_pcg_create_body(const help_pcg_options* opt, help_pcg** out) {
@@ -1015,7 +1016,8 @@ static int help_pcg_solve_body(help_pcg* ctx, const double* d, const double* b_1
     ctx->stats.cg_kernel_ms_total += ctx->solve_kernel_ms;
     ctx->stats.cg_iterations_fp32 = ctx->solve_iters_f32;
     ctx->stats.cg_launches = ctx->solve_launches;
-    if (!converged && !ctx->opt.fallback) return fail(ctx, HELP_E_NOT_CONVERGED, "solve: iteration cap reached");
+    if (!converged && !ctx->opt.cap_ok)
+        return fail(ctx, HELP_E_NOT_CONVERGED, "solve: CG stopped at its iteration cap before cg_tol");
     return HELP_OK;
 }
 

@@ -9,7 +9,10 @@
 // product needs -- the intermediate t = D^-1 A^T x of n entries -- lives in
 // the file-scope device array below.  It is a fixed kNoallocMaxCols doubles
 // (8 MiB); every GPU that loads this library holds it until the process
-// exits.
+// exits.  The CUDA runtime loads a library's device code lazily by default,
+// so the array is reserved by the first call on each device (that call takes
+// the 8 MiB of device memory): make it at start-up, before memory is handed
+// to the pool that forbids allocation and before any stream capture.
 //
 // The product is the same two row-gather passes as the backend's
 // HELP_OP_ADAT (spmv.cuh), here without a planned row split: every row is
@@ -17,7 +20,6 @@
 #include <cuda_runtime.h>
 
 #include <climits>
-#include <mutex>
 
 #include "../../include/help_gpu.h"
 #include "common.cuh"
@@ -27,34 +29,26 @@ namespace help {
 namespace {
 
 constexpr int kNoallocMaxCols = 1 << 20;  // largest n: 1,048,576 columns (8 MiB of doubles)
-constexpr int kNoallocMaxDevices = 64;
 constexpr int kNoallocThreads = 256;
 
 // Shared by every call on a device; holds the last call's intermediate t.
 __device__ __align__(256) double g_noalloc_t[kNoallocMaxCols];
 
-std::mutex g_mu;
-double* g_t_addr[kNoallocMaxDevices] = {nullptr};
-int g_num_sms[kNoallocMaxDevices] = {0};
-
-// Device address of g_noalloc_t on `dev` (the current device).  In host code
-// the symbol's name is only a host-side stand-in, so the address is asked of
-// the runtime once per device and kept.
+// Device address of g_noalloc_t on `dev` (the current device) and its SM
+// count.  In host code the symbol's name is only a host-side stand-in, so the
+// address is asked of the runtime on every call: after a cudaDeviceReset or
+// in another context on the same ordinal the module is loaded again, possibly
+// at another address, so a cached pointer could go stale.  Once the module is
+// loaded the lookup allocates nothing and costs well under a microsecond.
 int setup_device(int dev, double** t, int* num_sms) {
-    if (dev < 0 || dev >= kNoallocMaxDevices) return HELP_E_ARG;
-    std::lock_guard<std::mutex> lock(g_mu);
-    if (!g_t_addr[dev]) {
-        void* p = nullptr;
-        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_t);
-        if (e != cudaSuccess) return HELP_E_CUDA;
-        int sms = 0;
-        e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        if (e != cudaSuccess) return HELP_E_CUDA;
-        g_t_addr[dev] = static_cast<double*>(p);
-        g_num_sms[dev] = sms;
-    }
-    *t = g_t_addr[dev];
-    *num_sms = g_num_sms[dev];
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_t);
+    if (e != cudaSuccess) return HELP_E_CUDA;
+    int sms = 0;
+    e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) return HELP_E_CUDA;
+    *t = static_cast<double*>(p);
+    *num_sms = sms;
     return HELP_OK;
 }
 

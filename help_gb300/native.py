@@ -59,6 +59,7 @@ class PcgOptions(C.Structure):
         ("warm_start", C.c_int32),
         ("fallback", C.c_int32),
         ("cg_path", C.c_int32),
+        ("cap_ok", C.c_int32),
     ]
 
 

@@ -37,7 +37,9 @@ enum {
     HELP_E_NOMEM = -3,       /* device or host allocation failed                  */
     HELP_E_NUMERIC = -4,     /* non-positive / non-finite d, breakdown, NaN        */
     HELP_E_TIMEOUT = -5,     /* a device-side wait ran past its limit              */
-    HELP_E_NOT_CONVERGED = -6 /* iteration cap hit (only when fallback is disabled) */
+    HELP_E_NOT_CONVERGED = -6 /* the solve's last CG run stopped at its iteration cap
+                                 without meeting cg_tol (x_1, x_2 are still written);
+                                 HELP_OK instead when options.cap_ok is set          */
 };
 
 enum {
@@ -62,8 +64,8 @@ typedef struct help_pcg_options {
     /* warm start and fallback (the learned correction is attached separately,
        help_pcg_attach_mlp, and brings its own warm start) */
     int32_t warm_start;      /* 1: start CG from the previous solve's x_2 of this renew */
-    int32_t fallback;        /* 1: mixed form -- when FP32 refinement stalls or hits its
-                                cap, finish with plain FP64 PCG                          */
+    int32_t fallback;        /* mixed form only -- 1: when FP32 refinement stalls or hits
+                                its cap, finish with plain FP64 PCG; 0: stop there        */
     int32_t cg_path;         /* 0 auto: the shared-memory-resident cluster kernel when
                                 the vectors fit one cluster's shared memory (<= 64
                                 pivots, rows of <= 32 G nonzeros), else one thread-block
@@ -71,6 +73,10 @@ typedef struct help_pcg_options {
                                 multi-kernel graph; 1 always the graph; 2 the cluster
                                 kernel over L2; 3 the resident kernel where it fits
                                 (else as 0)                                              */
+    int32_t cap_ok;          /* 0 (default): a solve whose last CG run stopped at its
+                                iteration cap returns HELP_E_NOT_CONVERGED; 1: it returns
+                                HELP_OK and stats.converged = 0 (for callers that treat
+                                an inexact Newton direction as usable)                   */
 } help_pcg_options;
 
 typedef struct help_pcg_stats {
@@ -248,9 +254,11 @@ int help_pcg_features(help_pcg* ctx, int32_t slot, float* x);
  * doubles (8 MiB) that every GPU loading the library keeps until the process
  * exits.  No cudaMalloc, cudaFree or allocating library call is made.
  *   - n larger than 2^20 is rejected with HELP_E_ARG;
- *   - the first call on a device looks up that array's device address (once
- *     per device, that device current): make the first call before any
- *     stream capture;
+ *   - the CUDA runtime loads the library's device code on first use, so the
+ *     first call on each device is the one that reserves the array (8 MiB of
+ *     device memory taken then): make it at start-up, with that device
+ *     current, before any stream capture and before the memory pool that
+ *     forbids allocation is set up; later calls allocate nothing;
  *   - every call on a device shares the array, so calls that overlap on the
  *     GPU (other streams, other host threads) race: serialise them;
  *   - nothing has to start at zero: the first pass writes every entry of the

@@ -13,7 +13,11 @@ Fixtures (all instances come from the seeded generator in help_gb300):
   ref_hsd_small.npz every SolveLinearEquation call (d, b_1, b_2, x_1, x_2, CG
                     iterations) of the reference program solving a 50 x 150 LP.
   ref_hsd.json      the reference program's iteration table (P.Obj, D.Obj, gap,
-                    infeasibilities as printed) for three LPs incl. config 0.
+                    infeasibilities as printed) for three LPs incl. config 0,
+                    and its final iterate at full precision (status, iterations,
+                    objectives, gap, infeasibilities, tau, kappa; written by
+                    oracle/ref/ref_record.cpp when HSD_Main destructs the
+                    backend, HSDSolver.cpp:881).
 """
 from __future__ import annotations
 
@@ -105,6 +109,7 @@ def run_ref_program(lp, record: bool):
         env = dict(os.environ)
         if record:
             env["HELP_REF_RECORD"] = tmp
+        env["HELP_REF_FINAL"] = os.path.join(tmp, "final.txt")
         r = subprocess.run([ob.REF_BIN, mps], input="x\n", capture_output=True, text=True, cwd=tmp, env=env,
                            timeout=3600)
         rows = []
@@ -114,7 +119,12 @@ def run_ref_program(lp, record: bool):
                 rows.append([int(mm.group(1))] + [float(mm.group(i)) for i in range(2, 7)])
         solves = read_solves(os.path.join(tmp, "solves.bin")) if record else None
         status = [l for l in r.stdout.splitlines() if "Problem Status" in l]
-        return rows, solves, (status[0] if status else "")
+        final = {}
+        with open(env["HELP_REF_FINAL"]) as f:
+            for line in f:
+                key, val = line.split()
+                final[key] = int(val) if key in ("status", "iterations", "solves", "cg_iterations") else float(val)
+        return rows, solves, (status[0] if status else ""), final
 
 
 def hsd():
@@ -125,9 +135,10 @@ def hsd():
     for name, spec, seed in cases:
         lp = L.generate(spec, seed)
         record = name.startswith("random-50x150")
-        rows, solves, status = run_ref_program(lp, record)
+        rows, solves, status, final = run_ref_program(lp, record)
         tables[name] = {"m": lp.m, "n": lp.n, "seed": seed, "rows": rows, "status": status,
-                        "cg_iters": solves["iters"].tolist() if solves is not None else None}
+                        "cg_iters": solves["iters"].tolist() if solves is not None else None,
+                        "final": final}
         if solves is not None:
             np.savez_compressed(os.path.join(HERE, "ref_hsd_small.npz"), **solves)
         print(name, len(rows), "rows", status)

@@ -124,3 +124,38 @@ def test_ragged_matrix_product():
         g.RenewLinearEquation(d)
         y = g.matvec("ADAT", w)
     assert rel(y, (A / d) @ (A.T @ w)) < 1e-13
+
+
+def test_iteration_cap_is_an_error_unless_cap_ok():
+    """A solve whose CG stops at cg_max_iter before cg_tol returns
+    HELP_E_NOT_CONVERGED (x_1, x_2 still written); with cap_ok it returns
+    HELP_OK and stats.converged = 0.  The reference's CG has no cap
+    (PCG.cpp:333-394 runs until ||r|| < 1e-20 ||r0||)."""
+    from help_gb300 import lp as L, native
+
+    lp = L.generate(L.spec_random(300, 900, 5), 3)
+    rng = np.random.default_rng(3)
+    d = np.exp(rng.uniform(-3, 3, lp.n))
+    b1, b2 = rng.standard_normal(lp.n), rng.standard_normal(lp.m)
+    for precision in ("fp64", "mixed"):
+        with backend.GpuNormalEquations(pivots=4, precision=precision, cg_tol=1e-14, cg_max_iter=3,
+                                        inner_max_iter=3, ir_max_outer=1) as g:
+            g.LinearEquation_Construct(lp)
+            g.RenewLinearEquation(d)
+            with pytest.raises(backend.BackendError) as e:
+                g.SolveLinearEquation(d, b1, b2)
+            assert e.value.code == native.HELP_E_NOT_CONVERGED
+            assert g.stats()["converged"] == 0
+        with backend.GpuNormalEquations(pivots=4, precision=precision, cg_tol=1e-14, cg_max_iter=3,
+                                        inner_max_iter=3, ir_max_outer=1, cap_ok=True) as g:
+            g.LinearEquation_Construct(lp)
+            g.RenewLinearEquation(d)
+            x1, x2 = g.SolveLinearEquation(d, b1, b2)
+            st = g.stats()
+            assert st["converged"] == 0 and np.all(np.isfinite(x2)) and np.all(np.isfinite(x1))
+        # the same context solves fully when the cap allows it
+        with backend.GpuNormalEquations(pivots=4, precision=precision, cg_tol=1e-12, cg_max_iter=100000) as g:
+            g.LinearEquation_Construct(lp)
+            g.RenewLinearEquation(d)
+            g.SolveLinearEquation(d, b1, b2)
+            assert g.stats()["converged"] == 1

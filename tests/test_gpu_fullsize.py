@@ -1,5 +1,18 @@
-"""The benchmark's configurations at full size, through properties that hold
-whatever the size (the oracle is too slow there):
+"""The benchmark's configurations at full size (configs 1-4: up to 1.9M x 8M
+with 104M nonzeros, Zipf rows of ~43k entries in config 2, 4,000 linking rows
+of ~16k entries in config 4).
+
+Against the oracle (the reference's own loops restated, O(nnz) per product):
+  * A x, A^T y (CSRMV_N / CSRMV_T, Helper.cpp:57-81) to 1e-12 relative and
+    A D^-1 A^T v (CSRMV_T, scale, CSRMV_N) to 1e-11;
+  * diag(A D^-1 A^T) (PCG.cpp:41-46) to 1e-13, and the k largest of it --
+    the pivots at the configuration's own k -- exactly;
+  * at k = 8 given pivots: the Schur diagonal D_S (PCG.cpp:60-120) to 1e-9 of
+    diag(G), one preconditioner application (PCG.cpp:183-196) to 1e-8, and
+    10 CG iterations (PCG.cpp:333-394; tolerance 1e-30 so both run exactly 10)
+    to 1e-6 -- a small k keeps the oracle's O(k nnz) factor build in seconds.
+
+And through properties that hold whatever the size:
 
   * G = A D^-1 A^T is symmetric:      x . G y == y . G x
   * and linear:                      G (a x + b y) == a G x + b G y
@@ -18,6 +31,7 @@ import numpy as np
 import pytest
 
 from help_gb300 import backend, lp as L
+from oracle import bindings as ob
 
 pytestmark = pytest.mark.gpu
 
@@ -38,6 +52,57 @@ def system(request):
     g.RenewLinearEquation(d)
     yield config, lp, d, g, rng
     g.close()
+
+
+@pytest.fixture(scope="module")
+def csr(system):
+    config, lp, d, g, rng = system
+    return lp.csr()
+
+
+def test_products_match_oracle(system, csr):
+    config, lp, d, g, rng = system
+    rp, ci, v = csr
+    x, w = rng.standard_normal(lp.n), rng.standard_normal(lp.m)
+    assert rel(g.matvec("A", x), ob.csrmv_n(rp, ci, v, x, lp.m, lp.n)) < 1e-12
+    assert rel(g.matvec("AT", w), ob.csrmv_t(rp, ci, v, w, lp.m, lp.n)) < 1e-12
+    want = ob.csrmv_n(rp, ci, v, ob.csrmv_t(rp, ci, v, w, lp.m, lp.n) / d, lp.m, lp.n)
+    assert rel(g.matvec("ADAT", w), want) < 1e-11
+
+
+def test_diagonal_and_pivots_match_oracle(system, csr):
+    config, lp, d, g, rng = system
+    rp, ci, v = csr
+    piv, dg, ds = g.pivots()
+    dg_ref = ob.diag_adat(rp, ci, v, d, lp.m)
+    assert rel(dg, dg_ref) < 1e-13
+    assert len(piv) == L.config_pivots(config)
+    assert np.array_equal(piv, ob.topk(dg, len(piv)))
+
+
+def test_schur_precond_and_capped_cg_match_oracle(system, csr):
+    config, lp, d, g0, rng = system
+    rp, ci, v = csr
+    k, iters = 8, 10
+    b = rng.standard_normal(lp.m)
+    r = rng.standard_normal(lp.m)
+    with backend.GpuNormalEquations(pivots=k, cg_tol=1e-30, cg_max_iter=iters) as g:
+        g.LinearEquation_Construct(lp)
+        g.RenewLinearEquation(d)
+        piv, dg, ds = g.pivots()
+        z = g.precond_apply(r)
+        x, it = g.cg(b)
+    pc = ob.PartialCholesky(rp, ci, v, d, lp.m, lp.n, k, ob.PIVOT_GIVEN, piv)
+    non = np.ones(lp.m, bool)
+    non[piv] = False
+    ds_ref = pc.diag_s
+    good = non & (ds_ref > 1e-6 * dg)  # rows whose Schur diagonal is not pure cancellation
+    assert np.max(np.abs(ds[good] - ds_ref[good]) / dg[good]) < 1e-9
+    assert rel(z, pc.apply(r)) < 1e-8
+    del pc
+    xo, ito = ob.pcg(rp, ci, v, d, b, lp.m, lp.n, k, ob.PIVOT_GIVEN, piv, tol=1e-30, max_iter=iters)
+    assert it == ito == iters
+    assert rel(x, xo) < 1e-6
 
 
 def test_product_symmetric_and_linear(system):

@@ -95,6 +95,28 @@ def test_gpu_library_exports_every_declared_symbol():
         getattr(lib, s)
 
 
+def test_default_options_match_the_reference_and_the_header_layout():
+    """help_pcg_default_options runs without a GPU: the reference's PCG
+    settings (10 pivots, FP64, 1e-20; PCG.h:19-20), an iteration cap that is
+    an error by default (cap_ok = 0), and the ctypes mirror the same size as
+    the C struct (the C compiler's sizeof, from the header)."""
+    lib = native.gpu_lib()
+    o = native.PcgOptions()
+    C.memset(C.byref(o), 0x5A, C.sizeof(o))
+    lib.help_pcg_default_options(C.byref(o))
+    assert (o.pivots, o.precision, o.cg_tol, o.cap_ok, o.fallback) == (10, native.HELP_PREC_FP64, 1e-20, 0, 1)
+    with tempfile.TemporaryDirectory() as tmp:
+        src = os.path.join(tmp, "s.c")
+        with open(src, "w") as f:
+            f.write('#include "help_gpu.h"\n#include <stdio.h>\n'
+                    'int main(void){printf("%zu\\n", sizeof(help_pcg_options)); return 0;}\n')
+        exe = os.path.join(tmp, "s")
+        import subprocess
+        subprocess.run(["gcc", "-std=c99", "-I", os.path.join(ROOT, "include"), src, "-o", exe], check=True)
+        size = int(subprocess.run([exe], capture_output=True, text=True, check=True).stdout)
+    assert size == C.sizeof(native.PcgOptions)
+
+
 def test_lp_library_exports_every_declared_symbol():
     lib = C.CDLL(os.path.join(native.LIBDIR, "libhelp_lp.so"))
     for s in _declared("help_lp.h"):

@@ -157,6 +157,25 @@ def test_hsd_tables_match_reference_program(golden_dir):
             np.testing.assert_allclose(got[3:6], want[3:6], rtol=6e-2)
 
 
+def test_hsd_final_iterate_matches_reference_program_bitwise(golden_dir):
+    """The driver + oracle end where the reference program ended: status,
+    iteration and solve counts, total CG iterations, objectives, gap,
+    infeasibilities, tau and kappa, all bit for bit (the reference's values
+    read from its globals at HSD_Main's end, HSDSolver.cpp:881)."""
+    tables = json.load(open(os.path.join(golden_dir, "ref_hsd.json")))
+    for name in ("random-50x150-k5-seed1", "random-200x600-k5-seed2"):
+        t = tables[name]
+        ref = t["final"]
+        lp = L.generate(L.spec_random(t["m"], t["n"], 5), t["seed"])
+        ora = ob.OracleNormalEquations(pivots=10)
+        be = ora.ne_backend()
+        res = hsd.solve_lp(lp, be)
+        assert res["status"] == ref["status"] and res["iterations"] == ref["iterations"]
+        assert res["solves"] == ref["solves"]
+        for key in ("primal_obj", "dual_obj", "rel_gap", "primal_infeas", "dual_infeas", "tau", "kappa"):
+            assert res[key] == ref[key], (name, key, res[key], ref[key])
+
+
 @pytest.mark.skipif(not ob.ref_available(), reason="reference harness not built on this machine")
 def test_live_reference_random_instances():
     R = ob.ref()
