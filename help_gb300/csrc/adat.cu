@@ -10,8 +10,19 @@
 // generation order, with the multiply and add rounded separately as the
 // reference's loops do; columns come out sorted inside each row.
 //
-// Rows with more than kAdatCap contributions are rejected (the caller gets
-// an error): the normal-equations path never needs the explicit matrix.
+// Rows with more than kAdatCap contributions (the Zipf rows of a skewed
+// matrix, the dense linking rows of a block-angular one) take a second
+// kernel: one warp per heavy row walks the row's entries in order and, for
+// each, the column's entries k >= i, adding A_ij w_j A_kj into a dense
+// accumulator over the row's column range [i, kmax] -- the reference's own
+// dense per-thread accumulator (Helper.cpp:210-211, :350-377), in the same
+// order (one column at a time; inside a column every k is distinct, so the
+// lanes never add to the same entry) -- and marks k in a bitmap; the bitmap,
+// read word by word, gives the columns in increasing order.  Each warp has
+// its own accumulator slot in global memory (acc[R] doubles, stamp[R] ints
+// marking which row last wrote an entry, so nothing is cleared between rows,
+// and R/32 bitmap words cleared as they are read), R the widest heavy row's
+// range.
 #include "common.cuh"
 #include "kernels.h"
 
@@ -125,11 +136,130 @@ __global__ void k_adat(const int* __restrict__ rp, const int* __restrict__ ci, c
     }
 }
 
+// kmax of each heavy row: the last row of every column it touches (rows are
+// sorted inside columns), so its output columns lie in [i, kmax].
+__global__ void k_adat_heavy_range(const int* __restrict__ heavy, int nh, const int* __restrict__ rp,
+                                   const int* __restrict__ ci, const int* __restrict__ cp, const int* __restrict__ ri,
+                                   int* __restrict__ range) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (int h = blockIdx.x * nw + warp; h < nh; h += gridDim.x * nw) {
+        const int i = heavy[h];
+        int mx = i;
+        for (int e = rp[i] + lane; e < rp[i + 1]; e += 32) {
+            const int j = ci[e];
+            if (cp[j + 1] > cp[j]) mx = max(mx, ri[cp[j + 1] - 1]);
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+        if (lane == 0) range[h] = mx - i + 1;
+    }
+}
+
+// One warp per heavy row, slot = the warp's index in the grid (the grid has
+// at most `slots` warps).  Count pass: the number of distinct k.  Fill pass:
+// the sums, in the reference's order, and the sorted columns.
+template <bool FILL>
+__global__ void k_adat_heavy(const int* __restrict__ heavy, int nh, const int* __restrict__ rp,
+                             const int* __restrict__ ci, const double* __restrict__ av, const int* __restrict__ cp,
+                             const int* __restrict__ ri, const double* __restrict__ avT, const double* __restrict__ wv,
+                             double* acc_all, int* stamp_all, unsigned* bits_all, size_t R, int* __restrict__ hcnt,
+                             const int* __restrict__ out_rp, int* __restrict__ out_ci, double* __restrict__ out_v) {
+    const int lane = threadIdx.x & 31;
+    const int slot = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nslots = (gridDim.x * blockDim.x) >> 5;
+    const size_t words = (R + 31) / 32;
+    double* acc = acc_all + (size_t)slot * R;
+    int* stamp = stamp_all + (size_t)slot * R;
+    unsigned* bits = bits_all + (size_t)slot * words;
+    for (int h = slot; h < nh; h += nslots) {
+        const int i = heavy[h];
+        unsigned top = 0;  // highest offset touched + 1
+        for (int e = rp[i]; e < rp[i + 1]; ++e) {
+            const int j = ci[e];
+            const int qb = cp[j], qe = cp[j + 1];
+            int lo = qb, hi = qe;
+            while (lo < hi) {
+                const int mid = (lo + hi) >> 1;
+                if (ri[mid] < i) lo = mid + 1;
+                else hi = mid;
+            }
+            const double vd = FILL ? __dmul_rn(av[e], wv[j]) : 0.0;
+            for (int q = lo + lane; q < qe; q += 32) {
+                const unsigned o = (unsigned)(ri[q] - i);
+                atomicOr(bits + (o >> 5), 1u << (o & 31));
+                top = max(top, o + 1);
+                if (FILL) {
+                    double a = 0.0;  // the reference's accumulator starts at zero (Helper.cpp:355-356)
+                    if (__ldcg(stamp + o) == i) a = __ldcg(acc + o);
+                    __stcg(acc + o, __dadd_rn(a, __dmul_rn(vd, avT[q])));
+                    __stcg(stamp + o, i);
+                }
+            }
+            __syncwarp();
+        }
+#pragma unroll
+        for (int s = 16; s > 0; s >>= 1) top = max(top, __shfl_xor_sync(0xffffffffu, top, s));
+        __syncwarp();
+        const int nwords = (int)((top + 31) / 32);
+        int pos = FILL ? out_rp[i] : 0;
+        for (int w0 = 0; w0 < nwords; w0 += 32) {
+            const int wi = w0 + lane;
+            unsigned word = 0;
+            if (wi < nwords) {
+                word = __ldcg(bits + wi);
+                __stcg(bits + wi, 0u);
+            }
+            const int c = __popc(word);
+            int incl = c;
+#pragma unroll
+            for (int s = 1; s < 32; s <<= 1) {
+                const int t = __shfl_up_sync(0xffffffffu, incl, s);
+                if (lane >= s) incl += t;
+            }
+            if (FILL) {
+                int o = pos + incl - c;
+                while (word) {
+                    const int b = __ffs(word) - 1;
+                    word &= word - 1;
+                    const int off = wi * 32 + b;
+                    out_ci[o] = i + off;
+                    out_v[o] = __ldcg(acc + off);
+                    ++o;
+                }
+            }
+            pos += __shfl_sync(0xffffffffu, incl, 31);
+        }
+        if (!FILL && lane == 0) hcnt[h] = pos;
+        __syncwarp();
+    }
+}
+
 }  // namespace
+
+cudaError_t adat_heavy_range(const int* heavy, int nh, const int* rp, const int* ci, const int* cp, const int* ri,
+                             int* range, cudaStream_t st) {
+    const int blocks = (nh + 3) / 4 < 1024 ? (nh + 3) / 4 : 1024;
+    k_adat_heavy_range<<<blocks > 0 ? blocks : 1, 128, 0, st>>>(heavy, nh, rp, ci, cp, ri, range);
+    return cudaGetLastError();
+}
+
+cudaError_t adat_heavy(const int* heavy, int nh, const int* rp, const int* ci, const double* av, const int* cp,
+                       const int* ri, const double* avT, const double* wv, double* acc, int* stamp, unsigned* bits,
+                       size_t R, int slots, int* hcnt, const int* out_rp, int* out_ci, double* out_v, cudaStream_t st) {
+    // slots is a multiple of 4: 4 warps per block, every warp owns one slot
+    const int blocks = slots / 4;
+    if (out_ci)
+        k_adat_heavy<true><<<blocks, 128, 0, st>>>(heavy, nh, rp, ci, av, cp, ri, avT, wv, acc, stamp, bits, R, hcnt,
+                                                   out_rp, out_ci, out_v);
+    else
+        k_adat_heavy<false><<<blocks, 128, 0, st>>>(heavy, nh, rp, ci, av, cp, ri, avT, wv, acc, stamp, bits, R, hcnt,
+                                                    out_rp, out_ci, out_v);
+    return cudaGetLastError();
+}
 
 cudaError_t adat_count(const int* rp, const int* ci, const int* cp, const int* ri, int m, int* cnt, cudaStream_t st) {
     const size_t smem = (size_t)kAdatCap * 8 * kAdatWarps;
-    cudaError_t e = cudaFuncSetAttribute(k_adat<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e = raise_smem_limit((const void*)k_adat<false>, (int)smem);
     if (e != cudaSuccess) return e;
     const int blocks = (m + kAdatWarps - 1) / kAdatWarps < 4096 ? (m + kAdatWarps - 1) / kAdatWarps : 4096;
     k_adat<false><<<blocks > 0 ? blocks : 1, 32 * kAdatWarps, smem, st>>>(rp, ci, nullptr, cp, ri, nullptr, nullptr, m,
@@ -140,7 +270,7 @@ cudaError_t adat_count(const int* rp, const int* ci, const int* cp, const int* r
 cudaError_t adat_fill(const int* rp, const int* ci, const double* av, const int* cp, const int* ri, const double* avT,
                       const double* wv, int m, const int* out_rp, int* out_ci, double* out_v, cudaStream_t st) {
     const size_t smem = (size_t)kAdatCap * 16 * kAdatWarps;
-    cudaError_t e = cudaFuncSetAttribute(k_adat<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e = raise_smem_limit((const void*)k_adat<true>, (int)smem);
     if (e != cudaSuccess) return e;
     const int blocks = (m + kAdatWarps - 1) / kAdatWarps < 4096 ? (m + kAdatWarps - 1) / kAdatWarps : 4096;
     k_adat<true><<<blocks > 0 ? blocks : 1, 32 * kAdatWarps, smem, st>>>(rp, ci, av, cp, ri, avT, wv, m, nullptr,

@@ -1278,10 +1278,52 @@ static int help_adat_assemble_body(help_pcg* ctx, const double* w, int32_t* row_
     std::vector<int32_t> hc((size_t)m);
     CK(cudaMemcpyAsync(hc.data(), cnt, 4 * (size_t)m, cudaMemcpyDeviceToHost, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
+    // rows whose contributions overflow the per-warp sort: the heavy-row kernel
+    std::vector<int32_t> heavy;
+    for (int i = 0; i < m; ++i)
+        if (hc[i] < 0) heavy.push_back(i);
+    const int nh = (int)heavy.size();
+    int* d_heavy = nullptr;
+    int* d_hcnt = nullptr;
+    double* h_acc = nullptr;
+    int* h_stamp = nullptr;
+    unsigned* h_bits = nullptr;
+    size_t R = 0;
+    int slots = 0;
+    if (nh > 0) {
+        CK(ctx->adat_heavy_list.ensure(8 * (size_t)nh + 16));
+        d_heavy = ctx->adat_heavy_list.as<int>();
+        d_hcnt = d_heavy + nh + (nh & 1);
+        CK(cudaMemcpyAsync(d_heavy, heavy.data(), 4 * (size_t)nh, cudaMemcpyHostToDevice, ctx->stream));
+        CK(adat_heavy_range(d_heavy, nh, ctx->rp.as<int>(), ctx->ci.as<int>(), ctx->cp.as<int>(), ctx->ri.as<int>(),
+                            d_hcnt, ctx->stream));
+        std::vector<int32_t> hr((size_t)nh);
+        CK(cudaMemcpyAsync(hr.data(), d_hcnt, 4 * (size_t)nh, cudaMemcpyDeviceToHost, ctx->stream));
+        CK(cudaStreamSynchronize(ctx->stream));
+        for (int h = 0; h < nh; ++h) R = std::max(R, (size_t)hr[h]);
+        // one accumulator slot per warp: at most 2 warps per SM, and at most
+        // ~1 GiB of slots (acc + stamp + bitmap = 12.125 bytes per entry)
+        const size_t per_slot = 12 * R + 4 * ((R + 31) / 32) + 64;
+        size_t cap = ((size_t)1 << 30) / per_slot;
+        slots = (int)std::min<size_t>(std::min<size_t>((size_t)nh, (size_t)2 * ctx->num_sms), std::max<size_t>(cap, 1));
+        slots = (slots + 3) & ~3;
+        CK(ctx->adat_heavy_slots.ensure(per_slot * (size_t)slots + 256));
+        h_acc = ctx->adat_heavy_slots.as<double>();
+        h_stamp = reinterpret_cast<int*>(h_acc + (size_t)slots * R);
+        h_bits = reinterpret_cast<unsigned*>(h_stamp + (size_t)slots * R);
+        CK(cudaMemsetAsync(h_stamp, 0xFF, 4 * (size_t)slots * R, ctx->stream));
+        CK(cudaMemsetAsync(h_bits, 0, 4 * (size_t)slots * ((R + 31) / 32), ctx->stream));
+        CK(adat_heavy(d_heavy, nh, ctx->rp.as<int>(), ctx->ci.as<int>(), nullptr, ctx->cp.as<int>(),
+                      ctx->ri.as<int>(), nullptr, nullptr, h_acc, h_stamp, h_bits, R, slots, d_hcnt, nullptr, nullptr,
+                      nullptr, ctx->stream));
+        std::vector<int32_t> hh((size_t)nh);
+        CK(cudaMemcpyAsync(hh.data(), d_hcnt, 4 * (size_t)nh, cudaMemcpyDeviceToHost, ctx->stream));
+        CK(cudaStreamSynchronize(ctx->stream));
+        for (int h = 0; h < nh; ++h) hc[heavy[h]] = hh[h];
+    }
     int64_t total = 0;
     row_ptr[0] = 0;
     for (int i = 0; i < m; ++i) {
-        if (hc[i] < 0) return fail(ctx, HELP_E_ARG, "adat: a row has more contributions than the assembly supports");
         total += hc[i];
         if (total > 2147483647LL) return fail(ctx, HELP_E_ARG, "adat: result exceeds int32 indexing");
         row_ptr[i + 1] = (int32_t)total;
@@ -1295,6 +1337,12 @@ static int help_adat_assemble_body(help_pcg* ctx, const double* w, int32_t* row_
     CK(cudaMemcpyAsync(drp, row_ptr, 4 * ((size_t)m + 1), cudaMemcpyHostToDevice, ctx->stream));
     CK(adat_fill(ctx->rp.as<int>(), ctx->ci.as<int>(), ctx->av.as<double>(), ctx->cp.as<int>(), ctx->ri.as<int>(),
                  ctx->avT.as<double>(), ctx->res.as<double>(), m, drp, dci, dv, ctx->stream));
+    if (nh > 0) {
+        CK(cudaMemsetAsync(h_stamp, 0xFF, 4 * (size_t)slots * R, ctx->stream));
+        CK(adat_heavy(d_heavy, nh, ctx->rp.as<int>(), ctx->ci.as<int>(), ctx->av.as<double>(), ctx->cp.as<int>(),
+                      ctx->ri.as<int>(), ctx->avT.as<double>(), ctx->res.as<double>(), h_acc, h_stamp, h_bits, R, slots,
+                      d_hcnt, drp, dci, dv, ctx->stream));
+    }
     CK(cudaMemcpyAsync(col, dci, 4 * (size_t)total, cudaMemcpyDeviceToHost, ctx->stream));
     CK(cudaMemcpyAsync(val, dv, 8 * (size_t)total, cudaMemcpyDeviceToHost, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));

@@ -112,6 +112,7 @@ struct help_pcg {
     help::DevMem partials;
     help::DevMem ctrl;
     help::DevMem adat_tmp;
+    help::DevMem adat_heavy_list, adat_heavy_slots;  // heavy rows of the assembly and their accumulators
 
 
     const double* last_d = nullptr;

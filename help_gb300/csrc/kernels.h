@@ -10,6 +10,12 @@
 
 namespace help {
 
+// The dynamic shared-memory limit of a kernel is a property of the function
+// (per device), shared by every context and host thread in the process:
+// only ever raise it, so a context sizing a smaller system never lowers the
+// limit under another context's launch (or graph capture).
+cudaError_t raise_smem_limit(const void* fn, int bytes);
+
 struct TopkStateDev {
     unsigned long long prefix;  // high bits of the threshold key decided so far
     unsigned long long mask;
@@ -178,6 +184,15 @@ size_t dense_work_elems(int k);
 cudaError_t dense_spd_inverse(double* g11, double* W, double* work, int k, int* regularised, cudaStream_t st);
 
 // ---- explicit A diag(w) A^T (adat.cu)
+// Rows of A D A^T with more contributions than the per-warp shared-memory
+// sort holds: kmax - i + 1 per heavy row, then the count (out_ci == null) or
+// fill pass over dense accumulator slots (acc, stamp: slots x R; bits:
+// slots x ceil(R / 32) words, zero; stamp all -1 before the first use).
+cudaError_t adat_heavy_range(const int* heavy, int nh, const int* rp, const int* ci, const int* cp, const int* ri,
+                             int* range, cudaStream_t st);
+cudaError_t adat_heavy(const int* heavy, int nh, const int* rp, const int* ci, const double* av, const int* cp,
+                       const int* ri, const double* avT, const double* wv, double* acc, int* stamp, unsigned* bits,
+                       size_t R, int slots, int* hcnt, const int* out_rp, int* out_ci, double* out_v, cudaStream_t st);
 cudaError_t adat_count(const int* rp, const int* ci, const int* cp, const int* ri, int m, int* cnt,
                        cudaStream_t st);
 cudaError_t adat_fill(const int* rp, const int* ci, const double* av, const int* cp, const int* ri,

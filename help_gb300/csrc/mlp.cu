@@ -24,6 +24,7 @@
 
 #include "../../include/help_gpu.h"
 #include "common.cuh"
+#include "kernels.h"
 #include "mlp.h"
 
 namespace help {
@@ -407,7 +408,7 @@ cudaError_t mlp_forward(const __nv_bfloat16* X, long long rows, const MlpDevWeig
 }
 
 cudaError_t mlp_configure() {
-    return cudaFuncSetAttribute(k_mlp_bwd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(BwdSmem));
+    return raise_smem_limit((const void*)k_mlp_bwd, (int)sizeof(BwdSmem));
 }
 
 cudaError_t mlp_loss_grad(const __nv_bfloat16* X, long long rows, const MlpDevWeights* w, const float* out,

@@ -28,6 +28,9 @@
 // dot products, alpha/beta and the pivot-block work stay in double.
 #include <cooperative_groups.h>
 
+#include <map>
+#include <mutex>
+
 #include "common.cuh"
 #include "kernels.h"
 #include "spmv.cuh"
@@ -519,14 +522,27 @@ __global__ void __launch_bounds__(kClusterThreads) k_cg_cluster(const CgArgs<V> 
 
 }  // namespace
 
+cudaError_t raise_smem_limit(const void* fn, int bytes) {
+    static std::mutex mu;
+    static std::map<std::pair<const void*, int>, int> limit;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    std::lock_guard<std::mutex> lock(mu);
+    int& cur = limit[{fn, dev}];
+    if (bytes <= cur) return cudaSuccess;
+    e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    if (e == cudaSuccess) cur = bytes;
+    return e;
+}
+
 template <class V>
 cudaError_t cg_configure(int k_max) {
     const int smem = (k_max > 0 ? k_max : 1) * (int)sizeof(double);
-    cudaError_t e = cudaFuncSetAttribute(k_init<V>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_p4<V>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_c<V>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(k_p2<V>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(sizeof(V) * kStageA));
+    cudaError_t e = raise_smem_limit((const void*)k_init<V>, smem);
+    if (e == cudaSuccess) e = raise_smem_limit((const void*)k_p4<V>, smem);
+    if (e == cudaSuccess) e = raise_smem_limit((const void*)k_c<V>, smem);
+    if (e == cudaSuccess) e = raise_smem_limit((const void*)k_p2<V>, (int)(sizeof(V) * kStageA));
     return e;
 }
 
@@ -556,8 +572,7 @@ int cg_threads() { return kCgThreads; }
 template <class V>
 int cg_cluster_configure(int k_max) {
     const int smem = (k_max > 0 ? k_max : 1) * (int)sizeof(double);
-    if (cudaFuncSetAttribute(k_cg_cluster<V>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess)
-        return 0;
+    if (raise_smem_limit((const void*)k_cg_cluster<V>, smem) != cudaSuccess) return 0;
     for (int cs : {16, 8}) {
         if (cs > 8 && cudaFuncSetAttribute(k_cg_cluster<V>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) !=
                           cudaSuccess) {

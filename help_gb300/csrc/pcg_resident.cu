@@ -629,24 +629,6 @@ ResLayout resident_layout(int m, int n, int k, int cs, int vbytes, const int32_t
 
 // The kernel for a layout: FP64 always exchanges t through L2 (measured
 // faster), FP32 through shared memory where t fits there.
-// The dynamic shared-memory limit is a property of the function (per
-// device), shared by every context in the process: only ever raise it, so a
-// context sizing a smaller system never lowers the limit under another
-// context's launch.
-static cudaError_t raise_smem_limit(const void* fn, int bytes) {
-    static std::mutex mu;
-    static std::map<std::pair<const void*, int>, int> limit;
-    int dev = 0;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e != cudaSuccess) return e;
-    std::lock_guard<std::mutex> lock(mu);
-    int& cur = limit[{fn, dev}];
-    if (bytes <= cur) return cudaSuccess;
-    e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-    if (e == cudaSuccess) cur = bytes;
-    return e;
-}
-
 template <class V>
 const void* resident_fn(bool mat_smem, bool t_smem) {
     if constexpr (sizeof(V) == 8) {

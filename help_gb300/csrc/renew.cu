@@ -541,12 +541,12 @@ cudaError_t gcols_rows(int pass, const int* rp, const int* ci, const double* bv,
     if (blocks < 1) blocks = 1;
     cudaError_t e;
     if (pass == 0) {
-        e = cudaFuncSetAttribute(k_gcols_rows<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        e = raise_smem_limit((const void*)k_gcols_rows<0>, (int)smem);
         if (e != cudaSuccess) return e;
         k_gcols_rows<0><<<blocks, threads, smem, st>>>(rp, ci, bv, bp_ptr, bp_c, bp_v, pivpos, m, k, delta, cnt, c_rp,
                                                        c_ci, c_v, g11);
     } else {
-        e = cudaFuncSetAttribute(k_gcols_rows<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        e = raise_smem_limit((const void*)k_gcols_rows<1>, (int)smem);
         if (e != cudaSuccess) return e;
         k_gcols_rows<1><<<blocks, threads, smem, st>>>(rp, ci, bv, bp_ptr, bp_c, bp_v, pivpos, m, k, delta, cnt, c_rp,
                                                        c_ci, c_v, g11);
@@ -567,7 +567,7 @@ cudaError_t ct_count(const int* c_rp, const int* c_ci, int m, int k, int* blk_cn
     const int nblk = (m + kCtRows - 1) / kCtRows;
     const int warps = ct_warps(k);
     const size_t smem = (size_t)warps * k * sizeof(int);
-    cudaError_t e = cudaFuncSetAttribute(k_ct_count, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e = raise_smem_limit((const void*)k_ct_count, (int)smem);
     if (e != cudaSuccess) return e;
     const int blocks = (nblk + warps - 1) / warps;
     k_ct_count<<<blocks, warps * 32, smem, st>>>(c_rp, c_ci, m, k, nblk, blk_cnt);
@@ -579,7 +579,7 @@ cudaError_t ct_fill(const int* c_rp, const int* c_ci, const double* c_v, int m, 
     const int nblk = (m + kCtRows - 1) / kCtRows;
     const int warps = ct_warps(k);
     const size_t smem = (size_t)warps * k * sizeof(int);
-    cudaError_t e = cudaFuncSetAttribute(k_ct_fill, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e = raise_smem_limit((const void*)k_ct_fill, (int)smem);
     if (e != cudaSuccess) return e;
     const int blocks = (nblk + warps - 1) / warps;
     k_ct_fill<<<blocks, warps * 32, smem, st>>>(c_rp, c_ci, c_v, m, k, nblk, blk_off, ct_ci, ct_v);

@@ -140,6 +140,23 @@ def diag_adat(rp, ci, v, d, m, gamma=0.0, delta=0.0):
     return out
 
 
+def adat(rp, ci, v, col_ptr, row_ind, val, w, m, n):
+    """Upper triangle of A diag(w) A^T: ADAt_Allocate + ADAt_Calc restated
+    (Helper.cpp:215-377).  Returns (row_ptr, col, val) with the columns of
+    every row sorted (the restatement keeps the reference's pattern order;
+    the values are the reference's sums, in its order, unchanged)."""
+    orp = np.zeros(m + 1, np.int32)
+    nnz = lib().oracle_adat_symbolic(m, n, P(rp), P(ci), P(col_ptr), P(row_ind), P(orp), None)
+    ocol = np.zeros(max(nnz, 1), np.int32)
+    lib().oracle_adat_symbolic(m, n, P(rp), P(ci), P(col_ptr), P(row_ind), P(orp), P(ocol))
+    oval = np.zeros(max(nnz, 1))
+    lib().oracle_adat_numeric(m, n, P(rp), P(ci), P(v), P(col_ptr), P(row_ind), P(val), P(w), P(orp), P(ocol),
+                              P(oval))
+    row = np.repeat(np.arange(m, dtype=np.int64), np.diff(orp))
+    o = np.lexsort((ocol[:nnz], row))
+    return orp, ocol[:nnz][o], oval[:nnz][o]
+
+
 def topk(diag, k):
     m = len(diag)
     piv = np.zeros(max(k, 1), np.int32)

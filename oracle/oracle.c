@@ -9,6 +9,7 @@
 #include "oracle.h"
 
 #include <math.h>
+#include <pthread.h>
 #include <stdlib.h>
 #include <string.h>
 
@@ -122,27 +123,75 @@ int64_t oracle_adat_symbolic(int m, int n, const int* row_ptr, const int* col_in
 }
 
 /* Helper.cpp:331-348 (and the CSR-linked variant :350-377, same order). */
+/* One row of ADAt_Calc (Helper.cpp:350-377): the dense accumulator is zeroed
+ * on the row's pattern, each row entry walks its column from the row down,
+ * the pattern is read back. */
+static void adat_numeric_row(int i, const int* row_ptr, const int* col_ind, const double* val, const int* col_ptr,
+                             const int* row_ind, const double* valT, const double* d, const int* pat_ptr,
+                             const int* pat_col, const int* link, double* acc, double* out) {
+    for (int p = pat_ptr[i]; p < pat_ptr[i + 1]; p++) acc[pat_col[p]] = 0;
+    for (int p = row_ptr[i]; p < row_ptr[i + 1]; p++) {
+        const int j = col_ind[p];
+        const double vd = val[p] * d[j];
+        for (int q = link[p]; q < col_ptr[j + 1]; q++) acc[row_ind[q]] += vd * valT[q];
+    }
+    for (int p = pat_ptr[i]; p < pat_ptr[i + 1]; p++) out[p] = acc[pat_col[p]];
+}
+
 void oracle_adat_numeric(int m, int n, const int* row_ptr, const int* col_ind, const double* val,
                          const int* col_ptr, const int* row_ind, const double* valT, const double* d,
                          const int* pat_ptr, const int* pat_col, double* out) {
-    int* link = csr_to_csc_link(m, n, row_ptr, col_ind, col_ptr);
-    double* acc = (double*)malloc(sizeof(double) * (size_t)(m > 0 ? m : 1));
-    if (!link || !acc) {
-        free(link);
-        free(acc);
-        return;
+    oracle_adat_numeric_threads(m, n, row_ptr, col_ind, val, col_ptr, row_ind, valT, d, pat_ptr, pat_col, out, 1);
+}
+
+/* The reference runs ADAt_Calc's row loop under `omp parallel for` with one
+ * dense accumulator per thread (Helper.cpp:210-211, :352-356); here POSIX
+ * threads take chunks of 256 rows from a shared counter.  Rows are
+ * independent, so the result is the same for every thread count. */
+typedef struct {
+    int m;
+    const int *row_ptr, *col_ind, *col_ptr, *row_ind, *pat_ptr, *pat_col, *link;
+    const double *val, *valT, *d;
+    double* out;
+    int next;
+    int failed;
+} adat_job;
+
+static void* adat_worker(void* arg) {
+    adat_job* J = (adat_job*)arg;
+    double* acc = (double*)malloc(sizeof(double) * (size_t)(J->m > 0 ? J->m : 1));
+    if (!acc) {
+        __atomic_store_n(&J->failed, 1, __ATOMIC_RELAXED);
+        return NULL;
     }
-    for (int i = 0; i < m; i++) {
-        for (int p = pat_ptr[i]; p < pat_ptr[i + 1]; p++) acc[pat_col[p]] = 0;
-        for (int p = row_ptr[i]; p < row_ptr[i + 1]; p++) {
-            const int j = col_ind[p];
-            const double vd = val[p] * d[j];
-            for (int q = link[p]; q < col_ptr[j + 1]; q++) acc[row_ind[q]] += vd * valT[q];
-        }
-        for (int p = pat_ptr[i]; p < pat_ptr[i + 1]; p++) out[p] = acc[pat_col[p]];
+    for (;;) {
+        const int b = __atomic_fetch_add(&J->next, 256, __ATOMIC_RELAXED);
+        if (b >= J->m) break;
+        const int e = b + 256 < J->m ? b + 256 : J->m;
+        for (int i = b; i < e; i++)
+            adat_numeric_row(i, J->row_ptr, J->col_ind, J->val, J->col_ptr, J->row_ind, J->valT, J->d, J->pat_ptr,
+                             J->pat_col, J->link, acc, J->out);
     }
-    free(link);
     free(acc);
+    return NULL;
+}
+
+int oracle_adat_numeric_threads(int m, int n, const int* row_ptr, const int* col_ind, const double* val,
+                                const int* col_ptr, const int* row_ind, const double* valT, const double* d,
+                                const int* pat_ptr, const int* pat_col, double* out, int threads) {
+    int* link = csr_to_csc_link(m, n, row_ptr, col_ind, col_ptr);
+    if (!link) return -1;
+    adat_job J = {m, row_ptr, col_ind, col_ptr, row_ind, pat_ptr, pat_col, link, val, valT, d, out, 0, 0};
+    if (threads < 1) threads = 1;
+    if (threads > 256) threads = 256;
+    pthread_t tid[256];
+    int started = 0;
+    for (int t = 1; t < threads; t++)
+        if (pthread_create(&tid[started], NULL, adat_worker, &J) == 0) started++;
+    adat_worker(&J);
+    for (int t = 0; t < started; t++) pthread_join(tid[t], NULL);
+    free(link);
+    return J.failed ? -1 : started + 1;
 }
 
 /* ---------------------------------------------------------------- partial Cholesky */

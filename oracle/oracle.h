@@ -36,6 +36,11 @@ int64_t oracle_adat_symbolic(int m, int n, const int* row_ptr, const int* col_in
 void oracle_adat_numeric(int m, int n, const int* row_ptr, const int* col_ind, const double* val,
                          const int* col_ptr, const int* row_ind, const double* valT, const double* d,
                          const int* pat_ptr, const int* pat_col, double* out);
+/* The same with `threads` POSIX threads (the reference's OpenMP row loop);
+ * returns the threads used, -1 on allocation failure. */
+int oracle_adat_numeric_threads(int m, int n, const int* row_ptr, const int* col_ind, const double* val,
+                                const int* col_ptr, const int* row_ind, const double* valT, const double* d,
+                                const int* pat_ptr, const int* pat_col, double* out, int threads);
 
 /* Pivot rules for the partial Cholesky. */
 enum {

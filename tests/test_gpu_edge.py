@@ -159,3 +159,27 @@ def test_iteration_cap_is_an_error_unless_cap_ok():
             g.RenewLinearEquation(d)
             g.SolveLinearEquation(d, b1, b2)
             assert g.stats()["converged"] == 1
+
+
+def test_context_with_fewer_pivots_leaves_an_earlier_one_usable():
+    """Kernel launch limits (dynamic shared memory sized by the pivot count)
+    are per function, shared by every context: constructing a second
+    context with fewer pivots must not lower them under the first, whose
+    CG graph is captured afterwards."""
+    from help_gb300 import lp as L
+
+    lp = L.generate(L.spec_random(2000, 6000, 5), 5)
+    rng = np.random.default_rng(5)
+    d = np.exp(rng.uniform(-4, 4, lp.n))
+    b = rng.standard_normal(lp.m)
+    with backend.GpuNormalEquations(pivots=512, cg_tol=1e-10, cg_max_iter=20000, cg_path="graph") as big:
+        big.LinearEquation_Construct(lp)
+        big.RenewLinearEquation(d)
+        with backend.GpuNormalEquations(pivots=2, cg_tol=1e-10, cg_max_iter=20000, cg_path="graph") as small:
+            small.LinearEquation_Construct(lp)
+            small.RenewLinearEquation(d)
+            xs, _ = small.cg(b)
+        xb, _ = big.cg(b)
+        z = big.precond_apply(b)
+        gx = big.matvec("ADAT", xb)
+    assert rel(gx, b) < 1e-8 and rel(xb, xs) < 1e-6 and np.all(np.isfinite(z))
