@@ -42,6 +42,7 @@ import numpy as np  # noqa: E402
 
 METRIC = "SpMV HBM GB/s: (A D^-1 A^T) v, two CSR row-gather passes (IPM time to 1e-8 gap reported alongside)"
 WORKLOAD = "config 1: m=100000 n=400000, 8 nnz/col (3.2M nnz), d log-uniform [1e-8,1e8]"
+L2_NOTE = "flushed before every step (256 MB write)"
 
 
 def alg_bytes(m: int, n: int, nnz: int, elem: int) -> dict:
@@ -322,9 +323,9 @@ def spmv_large(steps: int, warmup: int, local: int) -> dict:
     return out
 
 
-def pcg_rate(config: int, iters: int, local: int) -> dict:
+def pcg_rate(config: int, iters: int, local: int, k: int | None = None) -> dict:
     """PCG iterations per second on the given configuration with its pivot
-    count, d log-uniform in [1e-8, 1e8]: one CG run of exactly `iters`
+    count (or k), d log-uniform in [1e-8, 1e8]: one CG run of exactly `iters`
     iterations (unreachable tolerance) in FP64 and one in FP32 (the mixed
     form's inner solver), timed on the device with CUDA events."""
     from help_gb300 import backend, lp as L
@@ -333,7 +334,7 @@ def pcg_rate(config: int, iters: int, local: int) -> dict:
     rng = np.random.default_rng(7)
     d = np.exp(rng.uniform(np.log(1e-8), np.log(1e8), lp.n))
     b = rng.standard_normal(lp.m)
-    k = L.config_pivots(config)
+    k = L.config_pivots(config) if k is None else k
     out = {}
     with backend.GpuNormalEquations(pivots=k, precision="mixed", cg_tol=1e-300, cg_max_iter=iters,
                                     device=local) as g:
@@ -349,6 +350,135 @@ def pcg_rate(config: int, iters: int, local: int) -> dict:
     out.update({"workload": "config %d: m=%d n=%d nnz=%d, k=%d, nnz(C)=%d" % (config, lp.m, lp.n, lp.nnz, k, st["nnz_c"]),
                 "renew_ms": round(renew_ms, 2),
                 "path": {1: "graph", 2: "single cluster", 3: "resident cluster"}.get(int(st["cg_path_used"]), "?")})
+    return out
+
+
+def cpu_pcg_rate(config: int, k: int, iters: int) -> dict:
+    """The reference's CG loop (PCG.cpp:296-395 with its partial-Cholesky
+    preconditioner, greedy pivots, PCG.cpp:38-196) restated in oracle/, one
+    core (the reference's PCG path is serial): `iters` iterations at an
+    unreachable tolerance on the same system as pcg_rate, the factor build
+    timed apart."""
+    from help_gb300 import lp as L
+    from oracle import bindings as ob
+
+    lp = L.make_lp(config, 0)
+    rng = np.random.default_rng(7)
+    d = np.exp(rng.uniform(np.log(1e-8), np.log(1e8), lp.n))
+    b = rng.standard_normal(lp.m)
+    rp, ci, v = lp.csr()
+    t0 = time.perf_counter()
+    pc = ob.PartialCholesky(rp, ci, v, d, lp.m, lp.n, k)
+    build = time.perf_counter() - t0
+    del pc
+    t0 = time.perf_counter()
+    _, it = ob.pcg(rp, ci, v, d, b, lp.m, lp.n, k, tol=1e-300, max_iter=iters)
+    tot = time.perf_counter() - t0
+    us = (tot - build) * 1e6 / max(it, 1)
+    return {"workload": "config %d: m=%d n=%d nnz=%d, k=%d" % (config, lp.m, lp.n, lp.nnz, k), "cores": 1,
+            "kind": "port", "iterations": int(it), "us_per_iteration": round(us, 1),
+            "iterations_per_s": round(1e6 / us, 1), "factor_build_s": round(build, 3)}
+
+
+def adat_assembly(config: int, local: int, threads: int) -> dict:
+    """The explicit upper triangle of A D^-1 A^T: the reference's
+    ADAt_Allocate (symbolic, serial) + ADAt_Calc (numeric, its OpenMP row
+    loop; Helper.cpp:215-377) restated in oracle/ on `threads` host cores,
+    beside the GPU assembly (help_adat_assemble: count pass, fill pass,
+    result copied to host arrays; wall time of the second of two calls),
+    checked equal bit for bit."""
+    from help_gb300 import backend, lp as L
+    from oracle import bindings as ob
+
+    lp = L.make_lp(config, 0)
+    rng = np.random.default_rng(3)
+    w = 1.0 / np.exp(rng.uniform(np.log(1e-8), np.log(1e8), lp.n))
+    rp, ci, v = lp.csr()
+    cpu = ob.adat_timed(rp, ci, v, lp.col_ptr, lp.row_ind, lp.val, w, lp.m, lp.n, threads)
+    with backend.GpuNormalEquations(pivots=1, device=local) as g:
+        g.LinearEquation_Construct(lp)
+        g.adat(w)
+        t0 = time.perf_counter()
+        grp, gcol, gval = g.adat(w)
+        gs = time.perf_counter() - t0
+    orp, ocol, oval = ob.adat(rp, ci, v, lp.col_ptr, lp.row_ind, lp.val, w, lp.m, lp.n)
+    same = bool(np.array_equal(grp, orp) and np.array_equal(gcol, ocol) and np.array_equal(gval, oval))
+    return {"workload": "config %d: m=%d n=%d nnz=%d" % (config, lp.m, lp.n, lp.nnz), "nnz_upper": cpu["nnz"],
+            "gpu_s": round(gs, 4), "cpu_numeric_s": round(cpu["numeric_s"], 4),
+            "cpu_symbolic_s": round(cpu["symbolic_s"], 4), "cpu_threads": cpu["threads"], "kind": "port",
+            "bitwise_equal": same}
+
+
+def _cpu_ipm_worker(conn, core: int | None) -> None:
+    """Spawned process: the HSD driver over the oracle backend (the
+    reference's UsePCG_CPU / PCG restated, 10 pivots, CG to 1e-10 as the GPU
+    runs) on the 2,000 x 6,000 LP, on one host core."""
+    try:
+        if core is not None and hasattr(os, "sched_setaffinity"):
+            os.sched_setaffinity(0, {core})
+        from help_gb300 import hsd, lp as L
+        from oracle import bindings as ob
+
+        lp = L.make_lp(0, 0)
+        ora = ob.OracleNormalEquations(pivots=10, tol=1e-10)
+        t0 = time.perf_counter()
+        r = hsd.solve_lp(lp, ora.ne_backend())
+        el = time.perf_counter() - t0
+        conn.send({"seconds": round(el, 2), "status": r["status"], "iterations": r["iterations"],
+                   "cg_iterations": ora.total_iters(), "primal_obj": r["primal_obj"], "rel_gap": r["rel_gap"],
+                   "cores": 1, "kind": "port", "core": core,
+                   "sample": "whole IPM to 1e-8 gap on config 0 (m=2000 n=6000), 10 pivots, CG tol 1e-10"})
+    except Exception as e:  # reported, not fatal
+        conn.send({"error": str(e)})
+    conn.close()
+
+
+def start_cpu_ipm():
+    import multiprocessing as mp
+
+    ctx = mp.get_context("spawn")
+    parent, child = ctx.Pipe(duplex=False)
+    cores = sorted(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else []
+    core = cores[-1] if len(cores) > 2 else None
+    p = ctx.Process(target=_cpu_ipm_worker, args=(child, core), daemon=True)
+    p.start()
+    child.close()
+    return p, parent
+
+
+def finish_cpu_ipm(handle, timeout: float = 600.0) -> dict:
+    p, conn = handle
+    out = conn.recv() if conn.poll(timeout) else {"error": "did not finish within %.0f s" % timeout}
+    p.join(5)
+    return out
+
+
+def ipm_large(params, local: int, caps: dict) -> dict:
+    """The interior-point method on the large configurations, plain FP64 PCG
+    against the learned + mixed form (FP32 CG in FP64 refinement with the
+    trained model attached), each under the same wall-clock cap: gap,
+    infeasibilities and CG iterations against time at every iteration, and
+    the time to a 1e-8 gap where one is reached.  Solves stop at 20,000 CG
+    iterations and hand back their inexact direction (cap_ok)."""
+    from help_gb300 import learned, lp as L
+
+    out = {}
+    for config, cap in caps.items():
+        lp = L.make_lp(config, 0)
+        k = L.config_pivots(config)
+        res = {"workload": "config %d: m=%d n=%d nnz=%d, k=%d" % (config, lp.m, lp.n, lp.nnz, k),
+               "cap_s": cap}
+        for arm, prm, prec in (("plain_fp64", None, "fp64"), ("learned_mixed", params, "mixed")):
+            try:
+                r = learned.evaluate(lp, k, prm, cg_tol=1e-10, device=local, precision=prec, max_seconds=cap,
+                                     cg_max_iter=20000, cap_ok=True, trace=True)
+                r["seconds"] = round(r["seconds"], 2)
+                r["time_to_1e-8_s"] = r["seconds"] if r["status"] == 0 and r["rel_gap"] <= 1e-8 else None
+                res[arm] = r
+            except Exception as e:
+                res[arm] = {"error": str(e)}
+        out["config%d" % config] = res
+        del lp
     return out
 
 
@@ -382,7 +512,7 @@ def learned_ablation() -> dict:
                      "obj_rel_diff": abs(a["primal_obj"] - b["primal_obj"]) / abs(a["primal_obj"]),
                      "fallbacks": b["learned_fallbacks"]})
     return {"train_rows": int(train["X"].shape[0]), "train_steps": 400, "train_seconds": round(train_s, 2),
-            "loss_first": losses[0], "loss_last": losses[-1], "held_out": runs}
+            "loss_first": losses[0], "loss_last": losses[-1], "held_out": runs}, params
 
 
 def presolve_time() -> dict:
@@ -410,40 +540,68 @@ def presolve_time() -> dict:
     return out
 
 
+def numpy_instance(m: int, n: int, per_col: int, seed: int):
+    """The configuration's generator recipe in numpy alone (for the reference
+    arm, which loads none of this project's libraries): `per_col` distinct
+    uniform-random rows per column, values N(0,1); returned as CSR."""
+    rng = np.random.default_rng(seed)
+    rows = rng.integers(0, m, (n, per_col))
+    while True:
+        rows.sort(axis=1)
+        dup = np.any(rows[:, 1:] == rows[:, :-1], axis=1)
+        if not dup.any():
+            break
+        rows[dup] = rng.integers(0, m, (int(dup.sum()), per_col))
+    r = rows.ravel()
+    col = np.repeat(np.arange(n), per_col)
+    val = rng.standard_normal(r.size)
+    order = np.lexsort((col, r))
+    rp = np.zeros(m + 1, np.int32)
+    np.cumsum(np.bincount(r, minlength=m), out=rp[1:])
+    return rp, col[order].astype(np.int32), np.ascontiguousarray(val[order])
+
+
+def bench_config(ws: int) -> dict:
+    return {"workload": WORKLOAD, "l2": L2_NOTE, "parallelism": "replicas" if ws > 1 else "single GPU"}
+
+
 def run_reference(args) -> None:
+    """The reference's own CPU loops for the path (CSRMV_T, the D^-1 scale and
+    CSRMV_N, Helper.cpp:57-81, PCG.cpp:346-358; restated in oracle/ -- the
+    reference's own build needs its sources, which the GPU host does not
+    have) on the same configuration, one core (those loops are serial)."""
     ws, rank, _ = dist_env()
     if rank != 0:
         return
-    from help_gb300 import lp as L
-
-    lp = L.make_lp(1, 0)
+    m, n = 100000, 400000
+    rp, ci, v = numpy_instance(m, n, 8, 0)
     rng = np.random.default_rng(0)
-    d = np.exp(rng.uniform(np.log(1e-8), np.log(1e8), lp.n))
+    d = np.exp(rng.uniform(np.log(1e-8), np.log(1e8), n))
     from oracle import bindings as ob
 
-    rp, ci, v = lp.csr()
-    x = rng.standard_normal(lp.m)
-    nb = alg_bytes(lp.m, lp.n, lp.nnz, 8)["step"] + 8 * lp.n
+    x = rng.standard_normal(m)
+    nb = alg_bytes(m, n, len(ci), 8)["step"] + 8 * n
     for _ in range(args.warmup):
-        t = ob.csrmv_t(rp, ci, v, x, lp.m, lp.n)
+        t = ob.csrmv_t(rp, ci, v, x, m, n)
         t /= d
-        ob.csrmv_n(rp, ci, v, t, lp.m, lp.n)
+        ob.csrmv_n(rp, ci, v, t, m, n)
     ts = []
     for _ in range(args.steps):
         t0 = time.perf_counter()
-        t = ob.csrmv_t(rp, ci, v, x, lp.m, lp.n)
+        t = ob.csrmv_t(rp, ci, v, x, m, n)
         t /= d
-        ob.csrmv_n(rp, ci, v, t, lp.m, lp.n)
+        ob.csrmv_n(rp, ci, v, t, m, n)
         ts.append(time.perf_counter() - t0)
     tot = sum(ts)
     val = nb * len(ts) / tot / 1e9
     out = {"metric": METRIC, "value": round(val, 3), "unit": "GB/s", "impl": "reference", "n_gpus": ws,
            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 * tot / len(ts), 4),
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-           "config": {"workload": WORKLOAD},
+           "config": bench_config(ws),
            "cpu_baseline": {"value": round(val, 3), "unit": "GB/s", "cores": 1, "kind": "port",
-                            "sample": "%d products; the reference's CSRMV_T, scale, CSRMV_N loops restated in "
-                                      "oracle/ (the reference's own build needs its sources, absent here)" % len(ts)},
+                            "sample": "%d products on the configuration's recipe generated in numpy; the "
+                                      "reference's CSRMV_T, scale, CSRMV_N loops restated in oracle/ (the "
+                                      "reference's own build needs its sources, absent on this host)" % len(ts)},
            "e2e": {"value": round(val, 3), "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out), flush=True)
 
@@ -459,6 +617,9 @@ def main() -> None:
     ap.add_argument("--pcg-configs", default="0,1", help="configurations whose PCG iteration rate is measured")
     ap.add_argument("--pcg-iters", type=int, default=500, help="CG iterations per rate measurement")
     ap.add_argument("--pcg-only", action="store_true", help="only the PCG iteration rates (profiling runs)")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baselines beyond the product loop")
+    ap.add_argument("--no-ipm-large", action="store_true", help="skip the capped IPM runs on configs 1 and 4")
+    ap.add_argument("--ipm-large-caps", default="1:25,4:45", help="config:seconds per arm of the capped IPM runs")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
@@ -472,11 +633,13 @@ def main() -> None:
         print(json.dumps({"pcg": out}), flush=True)
         return
 
+    ws, rank, local = dist_env()
+    cpu_ipm = start_cpu_ipm() if rank == 0 and not args.no_cpu and not args.no_ipm else None
+
     import torch
 
     from help_gb300 import backend, lp as L
 
-    ws, rank, local = dist_env()
     if ws > 1:
         import torch.distributed as dist
 
@@ -573,6 +736,7 @@ def main() -> None:
 
     extra = {}
     cpu = None
+    params = None
     if rank == 0:
         cpu = cpu_adat_baseline(lp, d, seconds=10.0)
         if not args.no_ipm:
@@ -581,9 +745,9 @@ def main() -> None:
             except Exception as e:  # reported, not fatal for the kernel line
                 extra["ipm"] = {"error": str(e)}
             try:
-                extra["learned"] = learned_ablation()
+                extra["learned"], params = learned_ablation()
             except Exception as e:
-                extra["learned"] = {"error": str(e)}
+                extra["learned"], params = {"error": str(e)}, None
             try:
                 extra["presolve"] = presolve_time()
             except Exception as e:
@@ -596,19 +760,45 @@ def main() -> None:
                 extra["pcg"]["config%d" % c] = pcg_rate(c, args.pcg_iters, local)
             except Exception as e:
                 extra["pcg"]["config%d" % c] = {"error": str(e)}
+        if not args.no_cpu:
+            # like for like with the reference's shipped pivot count (PCG.h:20)
+            try:
+                extra["pcg"]["config1_k10"] = pcg_rate(1, args.pcg_iters, local, k=10)
+            except Exception as e:
+                extra["pcg"]["config1_k10"] = {"error": str(e)}
+            cores = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else (os.cpu_count() or 1)
+            extra["cpu"] = {"host_cores": cores, "pcg_rate": {}}
+            for c, it in ((0, 2000), (1, 100)):
+                try:
+                    extra["cpu"]["pcg_rate"]["config%d_k10" % c] = cpu_pcg_rate(c, 10, it)
+                except Exception as e:
+                    extra["cpu"]["pcg_rate"]["config%d_k10" % c] = {"error": str(e)}
+            extra["adat_assembly"] = {}
+            for c in (1, 2):
+                try:
+                    extra["adat_assembly"]["config%d" % c] = adat_assembly(c, local, max(1, cores - 2))
+                except Exception as e:
+                    extra["adat_assembly"]["config%d" % c] = {"error": str(e)}
     if rank == 0 and not args.no_large:
         try:
             extra["spmv_large"] = spmv_large(max(3, args.steps // 3), 2, local)
         except Exception as e:
             extra["spmv_large"] = {"error": str(e)}
+    if rank == 0 and not args.no_ipm_large:
+        caps = {int(a): float(b) for a, b in (kv.split(":") for kv in args.ipm_large_caps.split(",") if kv)}
+        try:
+            extra["ipm_large"] = ipm_large(params, local, caps)
+        except Exception as e:
+            extra["ipm_large"] = {"error": str(e)}
+    if cpu_ipm is not None:
+        extra.setdefault("cpu", {})["ipm_config0"] = finish_cpu_ipm(cpu_ipm)
 
     if rank == 0:
         out = {
             "metric": METRIC, "value": round(value, 2), "unit": "GB/s", "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": round(step_ms, 5), "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded generator, config 1)",
-            "config": {"workload": WORKLOAD, "l2": "flushed before every step (256 MB write)",
-                       "parallelism": "replicas" if ws > 1 else "single GPU"},
+            "config": bench_config(ws),
             "roofline": roof,
             "fp32": {"value": round(ab32["step"] / (res["f32"]["step_ms"] * 1e-3) / 1e9, 2), "unit": "GB/s",
                      "ms_per_step": round(res["f32"]["step_ms"], 5),

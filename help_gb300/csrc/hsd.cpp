@@ -381,6 +381,7 @@ struct Hsd {
             std::printf("+------+------------------+------------------+----------+----------+----------+\n");
         }
         int Iter;
+        const double t_start = now_s();
         for (Iter = 0; Iter < opt->max_iterations; Iter++) {
             rho = std::max(mu / mu0, 1e-12);
             CalcNewtonParameters();
@@ -398,6 +399,10 @@ struct Hsd {
                 (relative_gap <= opt->gap_tol && primal_infeas <= opt->pinf_tol && dual_infeas <= opt->dinf_tol))
                 break;
             if (be_error) break;
+            if (opt->max_seconds > 0.0 && now_s() - t_start > opt->max_seconds) {
+                status = HSD_STATUS_ITER_LIMIT;  // a wall-clock cap the reference lacks
+                break;
+            }
             Renew();
             const double DOT = LinearEquationBottom();
             const double phi = 1.0;

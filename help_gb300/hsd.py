@@ -10,7 +10,7 @@ from . import native
 
 def solve_lp(lp, backend: native.NeBackend, *, verbose: bool = False, max_iterations: int = 10000,
              gap_tol: float = 1e-8, on_iter=None, want_solution: bool = False,
-             presolve_lindep: bool = False) -> dict:
+             presolve_lindep: bool = False, max_seconds: float = 0.0) -> dict:
     """Run HSD_Main (HSDSolver.cpp:869-883) on ``lp`` with ``backend``'s four entry points.
 
     Returns a dict with status, iterations, objective values, gap, infeasibilities,
@@ -25,6 +25,7 @@ def solve_lp(lp, backend: native.NeBackend, *, verbose: bool = False, max_iterat
     opt.gap_tol = gap_tol
     opt.verbose = int(verbose)
     opt.presolve_lindep = int(presolve_lindep)
+    opt.max_seconds = float(max_seconds)
     cb = None
     if on_iter is not None:
         def _cb(user, it, s6):

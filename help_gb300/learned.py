@@ -360,18 +360,29 @@ def train(data: dict, steps: int = 600, lr: float = 3e-3, seed: int = 0, device:
 
 
 def evaluate(lp, pivots: int, params: np.ndarray | None, cg_tol: float = 1e-10, device: int = 0,
-             precision: str = "fp64") -> dict:
+             precision: str = "fp64", max_seconds: float = 0.0, cg_max_iter: int = 200_000,
+             cap_ok: bool = False, trace: bool = False) -> dict:
     """One IPM run; with ``params`` the model is attached; precision "mixed"
-    runs the FP32-in-FP64-refinement form (refined to cg_tol)."""
+    runs the FP32-in-FP64-refinement form (refined to cg_tol).
+    ``max_seconds`` caps the run's wall time; ``cap_ok`` lets a solve that
+    stops at ``cg_max_iter`` hand back its inexact direction; ``trace``
+    records (seconds, rel gap, primal / dual infeasibility, CG iterations so
+    far) at every iteration."""
     from . import hsd
 
     mlp = Mlp(device, params) if params is not None else None
-    with GpuNormalEquations(pivots=pivots, cg_tol=cg_tol, cg_max_iter=200_000, device=device,
-                            precision=precision, ir_tol=cg_tol) as ne:
+    rows = []
+    with GpuNormalEquations(pivots=pivots, cg_tol=cg_tol, cg_max_iter=cg_max_iter, device=device,
+                            precision=precision, ir_tol=cg_tol, cap_ok=cap_ok) as ne:
         if mlp is not None:
             ne._check(ne.lib.help_pcg_attach_mlp(ne.ctx, mlp.h))
         t0 = time.perf_counter()
-        r = hsd.solve_lp(lp, ne.ne_backend())
+
+        def on_iter(it, s):
+            rows.append([round(time.perf_counter() - t0, 3), s[2], s[3], s[4],
+                         int(ne.stats()["cg_iterations_total"])])
+
+        r = hsd.solve_lp(lp, ne.ne_backend(), max_seconds=max_seconds, on_iter=on_iter if trace else None)
         wall = time.perf_counter() - t0
         st = ne.stats()
         if mlp is not None:
@@ -380,6 +391,10 @@ def evaluate(lp, pivots: int, params: np.ndarray | None, cg_tol: float = 1e-10, 
         mlp.close()
     if r["rc"] != 0:
         raise RuntimeError("IPM backend error (rc %d)" % r["rc"])
-    return {"status": r["status"], "iterations": r["iterations"], "primal_obj": r["primal_obj"],
-            "rel_gap": r["rel_gap"], "cg_iterations": int(st["cg_iterations_total"]), "seconds": wall,
-            "learned_fallbacks": int(st["learned_fallbacks"])}
+    out = {"status": r["status"], "iterations": r["iterations"], "primal_obj": r["primal_obj"],
+           "rel_gap": r["rel_gap"], "primal_infeas": r["primal_infeas"], "dual_infeas": r["dual_infeas"],
+           "cg_iterations": int(st["cg_iterations_total"]), "seconds": wall,
+           "learned_fallbacks": int(st["learned_fallbacks"])}
+    if trace:
+        out["trace"] = {"columns": ["s", "rel_gap", "primal_infeas", "dual_infeas", "cg_iterations"], "rows": rows}
+    return out

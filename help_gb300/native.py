@@ -153,6 +153,7 @@ class HsdOptions(C.Structure):
         ("on_iter", C.c_void_p),
         ("user", C.c_void_p),
         ("presolve_lindep", C.c_int32),
+        ("max_seconds", C.c_double),
     ]
 
 

@@ -157,6 +157,10 @@ typedef struct help_hsd_options {
      * matrix, y_out still has m entries (0 on the dropped rows).  Where the
      * presolve does not apply (its -4) the LP is solved as it is. */
     int32_t presolve_lindep;
+    /* Wall-clock cap in seconds (0: none; the reference has none): checked
+     * before each iteration's renew; when it has run out the driver stops
+     * with status 2, as at the iteration limit. */
+    double max_seconds;
 } help_hsd_options;
 
 typedef struct help_hsd_result {

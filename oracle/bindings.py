@@ -47,6 +47,8 @@ def lib():
         L.oracle_adat_symbolic.argtypes = [C.c_int, C.c_int, vp, vp, vp, vp, vp, vp]
         L.oracle_adat_symbolic.restype = C.c_int64
         L.oracle_adat_numeric.argtypes = [C.c_int, C.c_int] + [vp] * 10
+        L.oracle_adat_numeric_threads.argtypes = [C.c_int, C.c_int] + [vp] * 10 + [C.c_int]
+        L.oracle_adat_numeric_threads.restype = C.c_int
         L.oracle_pchol_build.argtypes = [C.c_int, C.c_int, vp, vp, vp, vp, C.c_double, C.c_double, C.c_int, C.c_int,
                                          vp, C.POINTER(Pchol)]
         L.oracle_pchol_free.argtypes = [C.POINTER(Pchol)]
@@ -155,6 +157,26 @@ def adat(rp, ci, v, col_ptr, row_ind, val, w, m, n):
     row = np.repeat(np.arange(m, dtype=np.int64), np.diff(orp))
     o = np.lexsort((ocol[:nnz], row))
     return orp, ocol[:nnz][o], oval[:nnz][o]
+
+
+def adat_timed(rp, ci, v, col_ptr, row_ind, val, w, m, n, threads):
+    """ADAt_Allocate (symbolic, one thread) then ADAt_Calc (numeric, the
+    reference's OpenMP row loop with `threads` threads), each timed; the
+    values in the restatement's pattern order."""
+    import time
+    t0 = time.perf_counter()
+    orp = np.zeros(m + 1, np.int32)
+    nnz = lib().oracle_adat_symbolic(m, n, P(rp), P(ci), P(col_ptr), P(row_ind), P(orp), None)
+    ocol = np.zeros(max(nnz, 1), np.int32)
+    lib().oracle_adat_symbolic(m, n, P(rp), P(ci), P(col_ptr), P(row_ind), P(orp), P(ocol))
+    t1 = time.perf_counter()
+    oval = np.zeros(max(nnz, 1))
+    used = lib().oracle_adat_numeric_threads(m, n, P(rp), P(ci), P(v), P(col_ptr), P(row_ind), P(val), P(w), P(orp),
+                                             P(ocol), P(oval), threads)
+    t2 = time.perf_counter()
+    if used < 0:
+        raise MemoryError("oracle_adat_numeric_threads")
+    return {"nnz": int(nnz), "symbolic_s": t1 - t0, "numeric_s": t2 - t1, "threads": int(used)}
 
 
 def topk(diag, k):

@@ -40,3 +40,25 @@ def test_presolve_entry():
     assert d["mcf_200x200x8_ungrounded"]["rows"] == 479200
     assert d["config1_random"]["result"].startswith("not applicable")
     assert d["mcf_200x200x8_ungrounded"]["s"] > 0 and d["config1_random"]["s"] > 0
+
+
+def test_reference_arm_loads_no_project_library_and_shares_the_config():
+    """The reference arm runs the reference's loops (restated in oracle/) on
+    an instance generated in numpy: none of this project's libraries is
+    loaded, and its config dict is the GPU arm's."""
+    code = ("import runpy, sys, io, contextlib, json; sys.argv = ['bench.py', '--impl', 'reference', '--steps', '1', "
+            "'--warmup', '1']; buf = io.StringIO()\n"
+            "with contextlib.redirect_stdout(buf):\n"
+            "    runpy.run_path('bench.py', run_name='__main__')\n"
+            "maps = open('/proc/self/maps').read()\n"
+            "print(json.dumps({'line': buf.getvalue(), 'help_libs': [l.split()[-1] for l in maps.splitlines() "
+            "if 'libhelp_' in l]}))")
+    r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, cwd=ROOT, timeout=600)
+    assert r.returncode == 0, r.stderr[-2000:]
+    out = json.loads(r.stdout.strip().splitlines()[-1])
+    assert out["help_libs"] == []
+    d = json.loads([ln for ln in out["line"].splitlines() if ln.startswith("{")][0])
+    sys.path.insert(0, ROOT)
+    import bench
+
+    assert d["config"] == bench.bench_config(1)

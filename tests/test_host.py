@@ -183,3 +183,15 @@ def test_hsd_driver_uses_backend_matvec():
     assert res["status"] == ref["status"] == 0
     assert calls.count(0) > 0 and calls.count(1) > 0
     assert abs(res["primal_obj"] - ref["primal_obj"]) <= 1e-9 * (1 + abs(ref["primal_obj"]))
+
+
+def test_hsd_driver_wall_clock_cap():
+    """max_seconds stops the driver before the next renew once it has run out
+    (status 2, as at the iteration limit); 0 means no cap."""
+    lp = L.generate(L.spec_random(300, 900, 5), 4)
+    ora = ob.OracleNormalEquations(pivots=10, tol=1e-10)
+    full = hsd.solve_lp(lp, ora.ne_backend())
+    assert full["status"] == 0
+    ora2 = ob.OracleNormalEquations(pivots=10, tol=1e-10)
+    capped = hsd.solve_lp(lp, ora2.ne_backend(), max_seconds=1e-9)
+    assert capped["status"] == 2 and capped["iterations"] == 1 and capped["renews"] <= 1

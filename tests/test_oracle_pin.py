@@ -193,3 +193,26 @@ def test_live_reference_random_instances():
         ox1, ox2 = ora.SolveLinearEquation(d, b1, b2)
         assert ora.last_iters() == it
         assert np.array_equal(ox1, x1) and np.array_equal(ox2, x2)
+
+
+def test_threaded_adat_calc_equals_serial():
+    """The threaded ADAt_Calc port (the reference's OpenMP row loop) gives the
+    serial restatement's values bit for bit, rows being independent."""
+    lp = L.generate(L.spec_zipf(3000, 12000, 6, 1.3, 70), 4)
+    rp, ci, v = lp.csr()
+    w = np.exp(np.random.default_rng(2).uniform(-2, 2, lp.n))
+    outs = []
+    for threads in (1, 4):
+        orp = np.zeros(lp.m + 1, np.int32)
+        nnz = ob.lib().oracle_adat_symbolic(lp.m, lp.n, ob.P(rp), ob.P(ci), ob.P(lp.col_ptr), ob.P(lp.row_ind),
+                                            ob.P(orp), None)
+        ocol = np.zeros(nnz, np.int32)
+        ob.lib().oracle_adat_symbolic(lp.m, lp.n, ob.P(rp), ob.P(ci), ob.P(lp.col_ptr), ob.P(lp.row_ind), ob.P(orp),
+                                      ob.P(ocol))
+        oval = np.zeros(nnz)
+        used = ob.lib().oracle_adat_numeric_threads(lp.m, lp.n, ob.P(rp), ob.P(ci), ob.P(v), ob.P(lp.col_ptr),
+                                                    ob.P(lp.row_ind), ob.P(lp.val), ob.P(w), ob.P(orp), ob.P(ocol),
+                                                    ob.P(oval), threads)
+        assert used == threads
+        outs.append(oval)
+    assert np.array_equal(outs[0], outs[1])
