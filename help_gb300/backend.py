@@ -49,7 +49,7 @@ class GpuNormalEquations:
                  cg_max_iter: int = 1_000_000, delta: float = 0.0, ir_tol: float = 1e-10,
                  ir_max_outer: int = 10, inner_tol: float = 1e-5, inner_max_iter: int = 200_000,
                  warm_start: bool = False, fallback: bool = True, device: int = 0, cg_path: str = "auto",
-                 cap_ok: bool = False):
+                 cap_ok: bool = False, mixed_max_d_spread: float = 1e8):
         self.lib = native.gpu_lib()
         o = native.PcgOptions()
         self.lib.help_pcg_default_options(C.byref(o))
@@ -67,6 +67,7 @@ class GpuNormalEquations:
         o.fallback = int(bool(fallback))
         o.cg_path = {"auto": 0, "graph": 1, "cluster": 2, "resident": 3}[cg_path]
         o.cap_ok = int(bool(cap_ok))
+        o.mixed_max_d_spread = float(mixed_max_d_spread)
         self.options = o
         h = C.c_void_p()
         self._check(self.lib.help_pcg_create(C.byref(o), C.byref(h)), None)

@@ -187,6 +187,19 @@ int resident_fits(const help_pcg* ctx, bool f32) {
     return ctx->resident_cs[slot];
 }
 
+// Whether an FP32 CG run would take the multi-kernel graph path, the one
+// that streams the matrix from HBM: on the resident and cluster paths an
+// iteration is bound by barrier and dependent-load latency, and FP32 saves
+// nothing there (measured: 12.0 against 11.4 us per iteration on config 0).
+bool fp32_on_graph(const help_pcg* ctx) {
+    const int p = ctx->opt.cg_path;
+    if (resident_fits(ctx, true) > 0 && (p == 0 || p == 3)) return false;
+    const int cs = ctx->cluster_cs[1];
+    if (cs > 0 && p == 2) return false;
+    if (cs > 0 && (p == 0 || p == 3) && cluster_work(ctx) <= kClusterWorkMax) return false;
+    return true;
+}
+
 int finish_pcg(help_pcg* ctx, bool f32, const CgScalars* h, CgResult* res) {
     CK(cudaEventSynchronize(ctx->ev1));
     float kms = 0.f;
@@ -373,10 +386,17 @@ int normal_solve(help_pcg* ctx, const double* rhs, double* x, bool warm, long lo
         *converged_out = res.converged;
         return HELP_OK;
     }
-    // Mixed precision: FP32 CG corrections inside FP64 iterative refinement.
-    // Once FP32 corrections stagnated (the interior-point iterates only get
-    // worse conditioned), later solves go straight to FP64 PCG.
+    // Mixed precision: FP32 CG corrections inside FP64 iterative refinement,
+    // where FP32 can pay -- chosen up front, per renew: the CG runs on the
+    // bandwidth-bound graph path, and max(d) / min(d) is at most
+    // mixed_max_d_spread (the FP32 operator is off by ~1e-7 relative, so
+    // FP32 CG stops converging once the normal equations' conditioning,
+    // which follows the spread of d, passes ~1e7-1e8).  Otherwise, and once
+    // FP32 corrections stagnated in this context (interior-point iterates
+    // only get worse conditioned), plain FP64 PCG to the same FP64 target.
     if (!warm) CK(vec_fill(x, 0.0, m, ctx->stream));
+    const bool use_fp32 = fp32_on_graph(ctx) && ctx->d_spread <= ctx->opt.mixed_max_d_spread && !ctx->fp32_stagnated;
+    ctx->stats.fp32_chosen = use_fp32 ? 1 : 0;
     double rr = 0.0;
     rc = residual_f64(ctx, x, rhs, r, &rr);
     if (rc) return rc;
@@ -384,7 +404,7 @@ int normal_solve(help_pcg* ctx, const double* rhs, double* x, bool warm, long lo
     int outer = 0;
     bool ok = (rr <= target2) || rhs2 == 0.0;
     double prev = rr;
-    while (!ok && !ctx->fp32_stagnated && outer < ctx->opt.ir_max_outer) {
+    while (!ok && use_fp32 && outer < ctx->opt.ir_max_outer) {
         // scale the residual to unit norm before narrowing to FP32
         const double scale = std::sqrt(rr);
         CK(vec_to_f32_scaled(r, 1.0 / scale, ctx->r032.as<float>(), m, ctx->stream));
@@ -406,13 +426,13 @@ int normal_solve(help_pcg* ctx, const double* rhs, double* x, bool warm, long lo
         prev = rr;
     }
     *outer_out = outer;
-    if (!ok && ctx->opt.fallback) {  // the mixed form's FP64 finish
+    if (!ok && (!use_fp32 || ctx->opt.fallback)) {  // FP64 chosen up front, or the mixed form's FP64 finish
         CgResult res;
         const double tol = (rr > 0.0) ? ctx->opt.ir_tol * std::sqrt(rhs2 / rr) : 1.0;
         rc = run_pcg<double>(ctx, x, r, std::min(tol, 1.0), ctx->opt.cg_max_iter, 0, &res);
         if (rc) return rc;
         iters += res.iterations;
-        *fell_back = 1;
+        *fell_back = use_fp32 ? 1 : 0;
         ok = res.converged != 0;
     }
     *iters_out = iters;
@@ -747,6 +767,7 @@ void help_pcg_default_options(help_pcg_options* o) {
     o->fallback = 1;
     o->cg_path = 0;
     o->cap_ok = 0;
+    o->mixed_max_d_spread = 1e8;
 }
 
 static int help_pcg_create_body(const help_pcg_options* opt, help_pcg** out) {
@@ -919,6 +940,15 @@ static int help_pcg_renew_body(help_pcg* ctx, const double* d) {
         return rc;
     }
     ctx->last_d = d;
+    // spread of d for the mixed form's choice (renew_impl has checked that
+    // every d is positive and finite)
+    double dmin = d[0], dmax = d[0];
+    for (int j = 1; j < ctx->n; ++j) {
+        dmin = std::min(dmin, d[j]);
+        dmax = std::max(dmax, d[j]);
+    }
+    ctx->d_spread = dmax / dmin;
+    ctx->stats.d_spread = ctx->d_spread;
     return HELP_OK;
 }
 

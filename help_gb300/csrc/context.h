@@ -118,6 +118,7 @@ struct help_pcg {
     const double* last_d = nullptr;
     bool have_prev_x2 = false;
     bool fp32_stagnated = false;      // mixed: FP32 refinement stalled once; FP64 from then on
+    double d_spread = 1.0;            // max(d) / min(d) of the last renew
 
     // learned part (mlp_api.cu): attached model, its per-renew inputs and
     // outputs, the uncorrected D_S^-1, and the solutions of the solve slots

@@ -60,6 +60,7 @@ class PcgOptions(C.Structure):
         ("fallback", C.c_int32),
         ("cg_path", C.c_int32),
         ("cap_ok", C.c_int32),
+        ("mixed_max_d_spread", C.c_double),
     ]
 
 
@@ -86,6 +87,8 @@ class PcgStats(C.Structure):
         ("cluster_ctas", C.c_int32),
         ("learned_warm", C.c_int32),
         ("learned_fallbacks", C.c_int32),
+        ("fp32_chosen", C.c_int32),
+        ("d_spread", C.c_double),
     ]
 
 

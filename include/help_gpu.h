@@ -77,6 +77,10 @@ typedef struct help_pcg_options {
                                 iteration cap returns HELP_E_NOT_CONVERGED; 1: it returns
                                 HELP_OK and stats.converged = 0 (for callers that treat
                                 an inexact Newton direction as usable)                   */
+    double mixed_max_d_spread; /* mixed form: FP32 refinement only while max(d)/min(d) of
+                                the renew is at most this (default 1e8) and the CG runs
+                                on the bandwidth-bound graph path; otherwise plain FP64
+                                PCG to ir_tol, chosen before any FP32 work              */
 } help_pcg_options;
 
 typedef struct help_pcg_stats {
@@ -101,6 +105,8 @@ typedef struct help_pcg_stats {
     int32_t cluster_ctas;        /* CTAs per cluster of the single-cluster path (0 = unavailable) */
     int32_t learned_warm;        /* last solve: started from the model's warm start     */
     int32_t learned_fallbacks;   /* since construct: model-assisted solves redone plain */
+    int32_t fp32_chosen;         /* last solve (mixed): 1 FP32 refinement ran, 0 FP64 up front */
+    double d_spread;             /* last renew: max(d) / min(d)                         */
 } help_pcg_stats;
 
 /* Fills *opt with the defaults (FP64, k = 10, cg_tol = 1e-20 as the reference). */

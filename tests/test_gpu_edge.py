@@ -183,3 +183,28 @@ def test_context_with_fewer_pivots_leaves_an_earlier_one_usable():
         z = big.precond_apply(b)
         gx = big.matvec("ADAT", xb)
     assert rel(gx, b) < 1e-8 and rel(xb, xs) < 1e-6 and np.all(np.isfinite(z))
+
+
+def test_mixed_form_chooses_fp32_only_where_it_can_pay():
+    """The mixed form runs FP32 refinement only on the bandwidth-bound graph
+    path and while max(d)/min(d) <= mixed_max_d_spread; otherwise it goes to
+    plain FP64 PCG up front.  Either way the FP64 residual meets ir_tol."""
+    from help_gb300 import lp as L
+
+    rng = np.random.default_rng(8)
+    big = L.generate(L.spec_random(20000, 80000, 8), 8)      # graph path
+    small = L.generate(L.spec_random(300, 900, 5), 8)        # resident path
+    cases = [(big, 1e2, "graph", 1), (big, 1e12, "graph", 0), (small, 1e2, "auto", 0)]
+    for lp, spread, path, want in cases:
+        d = np.exp(rng.uniform(0.0, np.log(spread), lp.n))
+        b1, b2 = rng.standard_normal(lp.n), rng.standard_normal(lp.m)
+        with backend.GpuNormalEquations(pivots=16, precision="mixed", ir_tol=1e-10, cg_tol=1e-10,
+                                        cg_path=path) as g:
+            g.LinearEquation_Construct(lp)
+            g.RenewLinearEquation(d)
+            g.SolveLinearEquation(d, b1, b2)
+            st = g.stats()
+        assert st["fp32_chosen"] == want, (lp.m, spread, st["fp32_chosen"])
+        assert abs(st["d_spread"] - d.max() / d.min()) <= 1e-12 * st["d_spread"]
+        assert st["rel_residual"] < 1e-9
+        assert (st["cg_iterations_fp32"] > 0) == bool(want)
