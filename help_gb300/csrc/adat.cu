@@ -156,8 +156,10 @@ __global__ void k_adat_heavy_range(const int* __restrict__ heavy, int nh, const 
 }
 
 // One warp per heavy row, slot = the warp's index in the grid (the grid has
-// at most `slots` warps).  Count pass: the number of distinct k.  Fill pass:
-// the sums, in the reference's order, and the sorted columns.
+// at most `slots` warps).  Count pass: the number of distinct k (lanes take
+// row entries; setting bits is order-free).  Fill pass: the sums, in the
+// reference's order (row entries one after another, lanes over a column's
+// entries), and the sorted columns.
 template <bool FILL>
 __global__ void k_adat_heavy(const int* __restrict__ heavy, int nh, const int* __restrict__ rp,
                              const int* __restrict__ ci, const double* __restrict__ av, const int* __restrict__ cp,
@@ -174,28 +176,59 @@ __global__ void k_adat_heavy(const int* __restrict__ heavy, int nh, const int* _
     for (int h = slot; h < nh; h += nslots) {
         const int i = heavy[h];
         unsigned top = 0;  // highest offset touched + 1
-        for (int e = rp[i]; e < rp[i + 1]; ++e) {
-            const int j = ci[e];
-            const int qb = cp[j], qe = cp[j + 1];
-            int lo = qb, hi = qe;
-            while (lo < hi) {
-                const int mid = (lo + hi) >> 1;
-                if (ri[mid] < i) lo = mid + 1;
-                else hi = mid;
-            }
-            const double vd = FILL ? __dmul_rn(av[e], wv[j]) : 0.0;
-            for (int q = lo + lane; q < qe; q += 32) {
-                const unsigned o = (unsigned)(ri[q] - i);
-                atomicOr(bits + (o >> 5), 1u << (o & 31));
-                top = max(top, o + 1);
-                if (FILL) {
-                    double a = 0.0;  // the reference's accumulator starts at zero (Helper.cpp:355-356)
-                    if (__ldcg(stamp + o) == i) a = __ldcg(acc + o);
-                    __stcg(acc + o, __dadd_rn(a, __dmul_rn(vd, avT[q])));
-                    __stcg(stamp + o, i);
+        if (!FILL) {
+            // the pattern does not depend on order: lanes take row entries
+            for (int e = rp[i] + lane; e < rp[i + 1]; e += 32) {
+                const int j = ci[e];
+                const int qb = cp[j], qe = cp[j + 1];
+                int lo = qb, hi = qe;
+                while (lo < hi) {
+                    const int mid = (lo + hi) >> 1;
+                    if (ri[mid] < i) lo = mid + 1;
+                    else hi = mid;
+                }
+                for (int q = lo; q < qe; ++q) {
+                    const unsigned o = (unsigned)(ri[q] - i);
+                    atomicOr(bits + (o >> 5), 1u << (o & 31));
+                    top = max(top, o + 1);
                 }
             }
-            __syncwarp();
+        }
+        // fill: row entries strictly in order; the column searches and the
+        // scaled values of 32 entries are found at once, one per lane, and
+        // broadcast entry by entry
+        for (int e0 = rp[i]; FILL && e0 < rp[i + 1]; e0 += 32) {
+            const int e = e0 + lane;
+            int lo = 0, qe = 0;
+            double vd = 0.0;
+            if (e < rp[i + 1]) {
+                const int j = ci[e];
+                int hi = cp[j + 1];
+                lo = cp[j];
+                qe = hi;
+                while (lo < hi) {
+                    const int mid = (lo + hi) >> 1;
+                    if (ri[mid] < i) lo = mid + 1;
+                    else hi = mid;
+                }
+                vd = __dmul_rn(av[e], wv[j]);
+            }
+            const int cnt = min(32, rp[i + 1] - e0);
+            for (int t = 0; t < cnt; ++t) {
+                const int lo_t = __shfl_sync(0xffffffffu, lo, t);
+                const int qe_t = __shfl_sync(0xffffffffu, qe, t);
+                const double vd_t = __shfl_sync(0xffffffffu, vd, t);
+                for (int q = lo_t + lane; q < qe_t; q += 32) {
+                    const unsigned o = (unsigned)(ri[q] - i);
+                    atomicOr(bits + (o >> 5), 1u << (o & 31));
+                    top = max(top, o + 1);
+                    double a = 0.0;  // the reference's accumulator starts at zero (Helper.cpp:355-356)
+                    if (__ldcg(stamp + o) == i) a = __ldcg(acc + o);
+                    __stcg(acc + o, __dadd_rn(a, __dmul_rn(vd_t, avT[q])));
+                    __stcg(stamp + o, i);
+                }
+                __syncwarp();
+            }
         }
 #pragma unroll
         for (int s = 16; s > 0; s >>= 1) top = max(top, __shfl_xor_sync(0xffffffffu, top, s));

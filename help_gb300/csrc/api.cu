@@ -52,8 +52,29 @@ double now_ms() {
 
 DevCtrl* ctrl_of(help_pcg* ctx) { return ctx->ctrl.as<DevCtrl>(); }
 
-int upload_split(help_pcg* ctx, RowSplit& S, const int32_t* ptr, int32_t rows, int g_min, int per_lane) {
+int upload_split(help_pcg* ctx, RowSplit& S, const int32_t* ptr, int32_t rows, int g_min, int per_lane,
+                 const int32_t* idx, size_t elem) {
     RowPlanHost h = plan_rows(ptr, rows, g_min, per_lane);
+    S.n_sell = 0;
+    if (idx) {
+        SellHost sh = plan_sell(ptr, idx, rows, h.short_max);
+        if (sh.nslices > 0) {
+            const size_t ne = sh.idx.size();
+            CK(S.sell_ptr.ensure(4 * sh.ptr.size()));
+            CK(S.sell_perm.ensure(4 * sh.perm.size()));
+            CK(S.sell_idx.ensure(4 * ne));
+            CK(S.sell_map.ensure(4 * ne));
+            CK(S.sell_val.ensure(elem * ne));
+            CK(cudaMemcpyAsync(S.sell_ptr.p, sh.ptr.data(), 4 * sh.ptr.size(), cudaMemcpyHostToDevice, ctx->stream));
+            CK(cudaMemcpyAsync(S.sell_perm.p, sh.perm.data(), 4 * sh.perm.size(), cudaMemcpyHostToDevice, ctx->stream));
+            CK(cudaMemcpyAsync(S.sell_idx.p, sh.idx.data(), 4 * ne, cudaMemcpyHostToDevice, ctx->stream));
+            CK(cudaMemcpyAsync(S.sell_map.p, sh.map.data(), 4 * ne, cudaMemcpyHostToDevice, ctx->stream));
+            CK(cudaStreamSynchronize(ctx->stream));  // sh goes out of scope
+            S.n_sell = sh.nslices;
+            S.sell_W = sh.W;
+            S.sell_entries = (int64_t)ne;
+        }
+    }
     S.G = h.G;
     S.short_max = h.short_max;
     S.n_med = (int32_t)h.med.size();
@@ -85,15 +106,43 @@ int upload_split(help_pcg* ctx, RowSplit& S, const int32_t* ptr, int32_t rows, i
     return HELP_OK;
 }
 
-int upload_plan(help_pcg* ctx, RowPlan& P, const int32_t* ptr, int32_t rows, bool with_f32) {
+// idx (host column indices, may be null): also lay the short rows out in
+// slices for B's products (A and A^T, whose B values are refreshed at renew)
+int upload_plan(help_pcg* ctx, RowPlan& P, const int32_t* ptr, int32_t rows, bool with_f32,
+                const int32_t* idx = nullptr) {
     P.rows = rows;
-    int rc = upload_split(ctx, P.s64, ptr, rows, kGminF64, kPerLaneF64);
-    if (!rc && with_f32) rc = upload_split(ctx, P.s32, ptr, rows, kGminF32, kPerLaneF32);
+    int rc = upload_split(ctx, P.s64, ptr, rows, kGminF64, kPerLaneF64, idx, 8);
+    if (!rc && with_f32) rc = upload_split(ctx, P.s32, ptr, rows, kGminF32, kPerLaneF32, idx, 4);
     return rc;
 }
 
+// B's values into the sliced layouts of A and A^T (both precisions present)
+int refresh_sell(help_pcg* ctx, bool mixed) {
+    const struct {
+        RowSplit* S;
+        const DevMem* src;
+        bool f32;
+    } jobs[4] = {{&ctx->pl_csr.s64, &ctx->bv, false},
+                 {&ctx->pl_csc.s64, &ctx->bvT, false},
+                 {&ctx->pl_csr.s32, &ctx->bv32, true},
+                 {&ctx->pl_csc.s32, &ctx->bvT32, true}};
+    for (const auto& j : jobs) {
+        if (j.f32 && !mixed) continue;
+        if (j.S->n_sell <= 0) continue;
+        if (j.f32)
+            CK(sell_gather<float>(j.S->sell_map.as<int>(), j.src->as<float>(), j.S->sell_val.as<float>(),
+                                  j.S->sell_entries, ctx->num_sms, ctx->stream));
+        else
+            CK(sell_gather<double>(j.S->sell_map.as<int>(), j.src->as<double>(), j.S->sell_val.as<double>(),
+                                   j.S->sell_entries, ctx->num_sms, ctx->stream));
+    }
+    return HELP_OK;
+}
+
+// sell: the value array is B's (bv / bvT / their FP32 copies), whose sliced
+// copy the split holds; other value arrays (A's own) take the CSR rows
 template <class V>
-SpmvView<V> view(const RowPlan& P, const DevMem& ptr, const DevMem& idx, const DevMem& val) {
+SpmvView<V> view(const RowPlan& P, const DevMem& ptr, const DevMem& idx, const DevMem& val, bool sell = false) {
     const RowSplit& S = std::is_same<V, float>::value ? P.s32 : P.s64;
     SpmvView<V> v;
     v.rows = P.rows;
@@ -114,6 +163,14 @@ SpmvView<V> view(const RowPlan& P, const DevMem& ptr, const DevMem& idx, const D
     v.parts = S.parts.as<double>();
     v.short_order = S.n_short > 0 ? S.sorder.as<int>() : nullptr;
     v.n_short = S.n_short;
+    if (sell && S.n_sell > 0) {
+        v.n_sell = S.n_sell;
+        v.sell_W = S.sell_W;
+        v.sell_ptr = S.sell_ptr.as<int>();
+        v.sell_perm = S.sell_perm.as<int>();
+        v.sell_idx = S.sell_idx.as<int>();
+        v.sell_val = S.sell_val.as<V>();
+    }
     return v;
 }
 
@@ -228,8 +285,8 @@ int run_pcg(help_pcg* ctx, V* x, V* r0, double tol, long long max_iter, int prec
     A.m = ctx->m;
     A.n = ctx->n;
     A.k = ctx->k;
-    A.csr = view<V>(ctx->pl_csr, ctx->rp, ctx->ci, f32 ? ctx->bv32 : ctx->bv);
-    A.csc = view<V>(ctx->pl_csc, ctx->cp, ctx->ri, f32 ? ctx->bvT32 : ctx->bvT);
+    A.csr = view<V>(ctx->pl_csr, ctx->rp, ctx->ci, f32 ? ctx->bv32 : ctx->bv, true);
+    A.csc = view<V>(ctx->pl_csc, ctx->cp, ctx->ri, f32 ? ctx->bvT32 : ctx->bvT, true);
     A.c = view<V>(ctx->pl_c, ctx->c_rp, ctx->c_ci, f32 ? ctx->c_v32 : ctx->c_v);
     A.ct = view<V>(ctx->pl_ct, ctx->ct_rp, ctx->ct_ci, f32 ? ctx->ct_v32 : ctx->ct_v);
     A.piv = ctx->piv.as<int>();
@@ -334,9 +391,9 @@ int run_pcg(help_pcg* ctx, V* x, V* r0, double tol, long long max_iter, int prec
 
 // res = rhs - G x  (FP64), returns ||res||^2 in *rr (host)
 int residual_f64(help_pcg* ctx, const double* x, const double* rhs, double* res, double* rr) {
-    CK(spmv_launch<double>(kEpiStore, view<double>(ctx->pl_csc, ctx->cp, ctx->ri, ctx->bvT), x, ctx->t.as<double>(),
+    CK(spmv_launch<double>(kEpiStore, view<double>(ctx->pl_csc, ctx->cp, ctx->ri, ctx->bvT, true), x, ctx->t.as<double>(),
                            nullptr, nullptr, nullptr, 0.0, spmv_blocks(ctx), kSpmvThreads, ctx->stream));
-    CK(spmv_launch<double>(kEpiResid, view<double>(ctx->pl_csr, ctx->rp, ctx->ci, ctx->bv), ctx->t.as<double>(), res,
+    CK(spmv_launch<double>(kEpiResid, view<double>(ctx->pl_csr, ctx->rp, ctx->ci, ctx->bv, true), ctx->t.as<double>(), res,
                            rhs, x, nullptr, ctx->opt.delta, spmv_blocks(ctx), kSpmvThreads, ctx->stream));
     if (rr) {
         double* part = ctx->partials.as<double>() + 4096;
@@ -588,9 +645,9 @@ int learned_warm_start(help_pcg* ctx, int slot, bool* used) {
     double* x = ctx->x.as<double>();
     double* gv = ctx->res.as<double>();
     CK(mlp_warm_vector(ctx->mlp_out.as<float>(), ctx->x2h[prev][slot].as<double>(), x, m, ctx->stream));
-    CK(spmv_launch<double>(kEpiStore, view<double>(ctx->pl_csc, ctx->cp, ctx->ri, ctx->bvT), x, ctx->t.as<double>(),
+    CK(spmv_launch<double>(kEpiStore, view<double>(ctx->pl_csc, ctx->cp, ctx->ri, ctx->bvT, true), x, ctx->t.as<double>(),
                            nullptr, nullptr, nullptr, 0.0, spmv_blocks(ctx), kSpmvThreads, ctx->stream));
-    CK(spmv_launch<double>(kEpiAddDelta, view<double>(ctx->pl_csr, ctx->rp, ctx->ci, ctx->bv), ctx->t.as<double>(), gv,
+    CK(spmv_launch<double>(kEpiAddDelta, view<double>(ctx->pl_csr, ctx->rp, ctx->ci, ctx->bv, true), ctx->t.as<double>(), gv,
                            x, nullptr, nullptr, ctx->opt.delta, spmv_blocks(ctx), kSpmvThreads, ctx->stream));
     double* part = ctx->partials.as<double>() + 4096;
     CK(vec_dot(x, ctx->rhs.as<double>(), m, part, part + 2049, ctx->stream));
@@ -627,6 +684,8 @@ int renew_impl(help_pcg* ctx, const double* d_host) {
                           ctx->avT.as<double>(), ctx->bvT.as<double>(), mixed ? ctx->bvT32.as<float>() : nullptr,
                           ctx->diag.as<double>(), ctx->opt.delta, m, n, ctx->nnz, &c->status, ctx->stream));
     rc = read_status(ctx, "renew: a row of A has no nonzeros, so A D^-1 A^T is singular (remove the row or set delta > 0)");
+    if (rc) return rc;
+    rc = refresh_sell(ctx, mixed);
     if (rc) return rc;
     // pivots
     const int k = std::max(0, std::min(ctx->opt.pivots, m));
@@ -885,8 +944,8 @@ static int help_pcg_construct_body(help_pcg* ctx, int32_t m, int32_t n, const in
     CK(cudaMemcpyAsync(ctx->ri.p, row_ind, 4 * (size_t)nnz, cudaMemcpyHostToDevice, ctx->stream));
     CK(cudaMemcpyAsync(ctx->avT.p, val, 8 * (size_t)nnz, cudaMemcpyHostToDevice, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
-    int rc = upload_plan(ctx, ctx->pl_csr, ctx->h_rp.data(), m, mixed);
-    if (!rc) rc = upload_plan(ctx, ctx->pl_csc, ctx->h_cp.data(), n, mixed);
+    int rc = upload_plan(ctx, ctx->pl_csr, ctx->h_rp.data(), m, mixed, ci.data());
+    if (!rc) rc = upload_plan(ctx, ctx->pl_csc, ctx->h_cp.data(), n, mixed, row_ind);
     if (!rc) rc = alloc_vectors(ctx);
     if (rc) return rc;
     // CG kernels: grid-stride, grid sized to the work (small problems pay
@@ -976,7 +1035,7 @@ static int help_pcg_solve_body(help_pcg* ctx, const double* d, const double* b_1
     if (rc) return rc;
     // u = D^-1/2 b_1 ;  rhs = B u - b_2 = A D^-1 b_1 - b_2   (UsePCG_CPU.cpp:103-112)
     CK(vec_scale_mul(ctx->s.as<double>(), ctx->b1.as<double>(), ctx->u.as<double>(), n, ctx->stream));
-    CK(spmv_launch<double>(kEpiRhs, view<double>(ctx->pl_csr, ctx->rp, ctx->ci, ctx->bv), ctx->u.as<double>(),
+    CK(spmv_launch<double>(kEpiRhs, view<double>(ctx->pl_csr, ctx->rp, ctx->ci, ctx->bv, true), ctx->u.as<double>(),
                            ctx->rhs.as<double>(), ctx->b2.as<double>(), nullptr, nullptr, 0.0, spmv_blocks(ctx),
                            kSpmvThreads, ctx->stream));
     // x_2 (UsePCG_CPU.cpp:154-166)
@@ -1027,7 +1086,7 @@ static int help_pcg_solve_body(help_pcg* ctx, const double* d, const double* b_1
     ctx->solve_slot++;
     ctx->stats.learned_warm = learned_warm ? 1 : 0;
     // x_1 = D^-1 (b_1 - A^T x_2) = D^-1/2 (u - B^T x_2)   (UsePCG_CPU.cpp:171-177)
-    CK(spmv_launch<double>(kEpiBacksub, view<double>(ctx->pl_csc, ctx->cp, ctx->ri, ctx->bvT), ctx->x.as<double>(),
+    CK(spmv_launch<double>(kEpiBacksub, view<double>(ctx->pl_csc, ctx->cp, ctx->ri, ctx->bvT, true), ctx->x.as<double>(),
                            ctx->x1.as<double>(), ctx->u.as<double>(), nullptr, ctx->s.as<double>(), 0.0,
                            spmv_blocks(ctx), kSpmvThreads, ctx->stream));
     rc = d2h(ctx, x_1, ctx->x1.as<double>(), n);
@@ -1084,13 +1143,13 @@ static int help_pcg_matvec_dev_body(help_pcg* ctx, int32_t op, int32_t fp32, con
     if (op == HELP_OP_B || op == HELP_OP_BT) {
         const bool t = op == HELP_OP_BT;
         if (fp32) {
-            const SpmvView<float> M = t ? view<float>(ctx->pl_csc, ctx->cp, ctx->ri, ctx->bvT32)
-                                        : view<float>(ctx->pl_csr, ctx->rp, ctx->ci, ctx->bv32);
+            const SpmvView<float> M = t ? view<float>(ctx->pl_csc, ctx->cp, ctx->ri, ctx->bvT32, true)
+                                        : view<float>(ctx->pl_csr, ctx->rp, ctx->ci, ctx->bv32, true);
             CK(spmv_launch<float>(kEpiStore, M, (const float*)x, (float*)y, nullptr, nullptr, nullptr, 0.0, nb,
                                   kSpmvThreads, st));
         } else {
-            const SpmvView<double> M = t ? view<double>(ctx->pl_csc, ctx->cp, ctx->ri, ctx->bvT)
-                                         : view<double>(ctx->pl_csr, ctx->rp, ctx->ci, ctx->bv);
+            const SpmvView<double> M = t ? view<double>(ctx->pl_csc, ctx->cp, ctx->ri, ctx->bvT, true)
+                                         : view<double>(ctx->pl_csr, ctx->rp, ctx->ci, ctx->bv, true);
             CK(spmv_launch<double>(kEpiStore, M, (const double*)x, (double*)y, nullptr, nullptr, nullptr, 0.0, nb,
                                    kSpmvThreads, st));
         }
@@ -1098,14 +1157,14 @@ static int help_pcg_matvec_dev_body(help_pcg* ctx, int32_t op, int32_t fp32, con
     }
     if (op != HELP_OP_ADAT) return fail(ctx, HELP_E_ARG, "matvec: unknown op");
     if (fp32) {
-        CK(spmv_launch<float>(kEpiStore, view<float>(ctx->pl_csc, ctx->cp, ctx->ri, ctx->bvT32), (const float*)x,
+        CK(spmv_launch<float>(kEpiStore, view<float>(ctx->pl_csc, ctx->cp, ctx->ri, ctx->bvT32, true), (const float*)x,
                               ctx->t32.as<float>(), nullptr, nullptr, nullptr, 0.0, nb, kSpmvThreads, st));
-        CK(spmv_launch<float>(kEpiAddDelta, view<float>(ctx->pl_csr, ctx->rp, ctx->ci, ctx->bv32), ctx->t32.as<float>(),
+        CK(spmv_launch<float>(kEpiAddDelta, view<float>(ctx->pl_csr, ctx->rp, ctx->ci, ctx->bv32, true), ctx->t32.as<float>(),
                               (float*)y, (const float*)x, nullptr, nullptr, ctx->opt.delta, nb, kSpmvThreads, st));
     } else {
-        CK(spmv_launch<double>(kEpiStore, view<double>(ctx->pl_csc, ctx->cp, ctx->ri, ctx->bvT), (const double*)x,
+        CK(spmv_launch<double>(kEpiStore, view<double>(ctx->pl_csc, ctx->cp, ctx->ri, ctx->bvT, true), (const double*)x,
                                ctx->t.as<double>(), nullptr, nullptr, nullptr, 0.0, nb, kSpmvThreads, st));
-        CK(spmv_launch<double>(kEpiAddDelta, view<double>(ctx->pl_csr, ctx->rp, ctx->ci, ctx->bv), ctx->t.as<double>(),
+        CK(spmv_launch<double>(kEpiAddDelta, view<double>(ctx->pl_csr, ctx->rp, ctx->ci, ctx->bv, true), ctx->t.as<double>(),
                                (double*)y, (const double*)x, nullptr, nullptr, ctx->opt.delta, nb, kSpmvThreads, st));
     }
     return HELP_OK;

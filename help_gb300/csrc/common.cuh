@@ -29,6 +29,34 @@ HELP_DEVINL T ld_ro(const T* p) {
     return __ldg(p);
 }
 
+// Streamed once per kernel (a matrix's indices and values): non-coherent
+// path without allocating in L1, so L1 keeps the gathered vector's lines.
+HELP_DEVINL int2 ld_stream_na(const int2* p) {
+    int2 v;
+    asm("ld.global.nc.L1::no_allocate.v2.s32 {%0,%1}, [%2];" : "=r"(v.x), "=r"(v.y) : "l"(p));
+    return v;
+}
+HELP_DEVINL double2 ld_stream_na(const double2* p) {
+    double2 v;
+    asm("ld.global.nc.L1::no_allocate.v2.f64 {%0,%1}, [%2];" : "=d"(v.x), "=d"(v.y) : "l"(p));
+    return v;
+}
+HELP_DEVINL float2 ld_stream_na(const float2* p) {
+    float2 v;
+    asm("ld.global.nc.L1::no_allocate.v2.f32 {%0,%1}, [%2];" : "=f"(v.x), "=f"(v.y) : "l"(p));
+    return v;
+}
+template <class V>
+struct Vec2;
+template <>
+struct Vec2<double> {
+    using T = double2;
+};
+template <>
+struct Vec2<float> {
+    using T = float2;
+};
+
 // Status codes a kernel can leave in its status word (mirror HELP_E_*).
 constexpr int kStatusOk = 0;
 constexpr int kStatusTimeout = -5;

@@ -45,6 +45,11 @@ struct RowSplit {
     DevMem seg, lnseg, lbase, tickets, parts;  // segments of long rows (items.h)
     DevMem sorder;                             // short rows in processing order (when uneven)
     int32_t G = 1, short_max = 32, n_med = 0, n_long = 0, n_seg = 0, n_short = 0;
+    // sliced layout of the short rows (items.h, SellHost), for B = A D^-1/2:
+    // its values (this split's precision) are refreshed from B at each renew
+    DevMem sell_ptr, sell_perm, sell_idx, sell_map, sell_val;
+    int32_t n_sell = 0, sell_W = 1;
+    int64_t sell_entries = 0;
 };
 struct RowPlan {
     int32_t rows = 0;

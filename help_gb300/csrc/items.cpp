@@ -94,4 +94,60 @@ RowPlanHost plan_rows(const int32_t* ptr, int32_t rows, int32_t g_min, int32_t p
     return p;
 }
 
+SellHost plan_sell(const int32_t* ptr, const int32_t* idx, int32_t rows, int32_t short_max) {
+    SellHost h;
+    std::vector<int32_t> order, win;
+    order.reserve((size_t)rows);
+    for (int32_t w0 = 0; w0 < rows; w0 += kOrderWindow) {
+        win.clear();
+        for (int32_t r = w0; r < std::min(rows, w0 + kOrderWindow); ++r)
+            if (ptr[r + 1] - ptr[r] <= short_max) win.push_back(r);
+        std::stable_sort(win.begin(), win.end(),
+                         [&](int32_t a, int32_t b) { return ptr[a + 1] - ptr[a] > ptr[b + 1] - ptr[b]; });
+        order.insert(order.end(), win.begin(), win.end());
+    }
+    if (order.empty()) return h;
+    const int64_t ns = ((int64_t)order.size() + 31) / 32;
+    std::vector<int32_t> sp((size_t)ns + 1);
+    int64_t tot = 0, len_sum = 0;
+    for (int64_t s = 0; s < ns; ++s) {
+        int32_t mx = 0;
+        for (int64_t q = 32 * s; q < std::min<int64_t>((int64_t)order.size(), 32 * s + 32); ++q)
+            mx = std::max(mx, ptr[order[q] + 1] - ptr[order[q]]);
+        mx = (mx + kSellStep - 1) / kSellStep * kSellStep;
+        if (tot > (int64_t)0x7fffffff - 32 * (int64_t)mx) return SellHost();
+        sp[(size_t)s] = (int32_t)tot;
+        tot += 32 * (int64_t)mx;
+        len_sum += mx;
+    }
+    sp[(size_t)ns] = (int32_t)tot;
+    h.nslices = (int32_t)ns;
+    const double mean = (double)len_sum / (double)ns;
+    while (h.W < 8 && 8.0 * (h.W * 2) <= mean) h.W *= 2;
+    h.ptr = std::move(sp);
+    h.perm.assign((size_t)ns * 32, -1);
+    h.idx.assign((size_t)tot, 0);
+    h.map.assign((size_t)tot, -1);
+    for (int64_t s = 0; s < ns; ++s) {
+        const int64_t base = h.ptr[(size_t)s], len = (h.ptr[(size_t)s + 1] - base) / 32;
+        for (int32_t r = 0; r < 32; ++r) {
+            const int64_t q = 32 * s + r;
+            if (q >= (int64_t)order.size()) break;
+            const int32_t row = order[(size_t)q], b = ptr[row], n = ptr[row + 1] - b;
+            h.perm[(size_t)q] = row;
+            const int32_t pad_col = n > 0 ? idx[b + n - 1] : 0;
+            for (int64_t j = 0; j < len; ++j) {
+                const int64_t at = base + (j / kSellStep) * 32 * kSellStep + r * kSellStep + j % kSellStep;
+                if (j < n) {
+                    h.idx[(size_t)at] = idx[b + j];
+                    h.map[(size_t)at] = b + (int32_t)j;
+                } else {
+                    h.idx[(size_t)at] = pad_col;
+                }
+            }
+        }
+    }
+    return h;
+}
+
 }  // namespace help

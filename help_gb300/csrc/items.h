@@ -30,4 +30,24 @@ constexpr double kOrderWaste = 1.5;    // reorder when index order wastes this f
 // g_min: smallest group; per_lane: target nonzeros per lane of an average row.
 RowPlanHost plan_rows(const int32_t* ptr, int32_t rows, int32_t g_min, int32_t per_lane);
 
+// Sliced layout of the short rows (length <= short_max) of one CSR matrix:
+// rows taken by decreasing length within windows of kOrderWindow rows, 32
+// per slice (one lane each), every slice padded to its longest row (rounded
+// up to kSellStep); entry j of the row in lane r of slice s sits at
+//   ptr[s] + (j / kSellStep) * 32 * kSellStep + r * kSellStep + j % kSellStep,
+// so a lane reads kSellStep consecutive entries with one vector load and a
+// warp's loads are contiguous.  perm[32 s + r] is the row (-1: no row); map
+// holds each entry's CSR position (-1: padding, value 0, index repeating the
+// row's last column).  W warps share a slice (each takes every W-th step
+// block) when slices are long: W = largest power of two <= mean slice
+// length / 8, at most 8.
+struct SellHost {
+    int32_t nslices = 0, W = 1;
+    std::vector<int32_t> ptr, perm, idx, map;
+};
+constexpr int32_t kSellStep = 2;
+// Empty result (nslices = 0) when there are no short rows or the layout
+// would pass 2^31 entries.
+SellHost plan_sell(const int32_t* ptr, const int32_t* idx, int32_t rows, int32_t short_max);
+
 }  // namespace help

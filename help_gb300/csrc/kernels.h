@@ -126,6 +126,9 @@ cudaError_t spmv_launch(int epi, const SpmvView<V>& M, const V* x, V* y, const V
 
 // ---- vector kernels (vec.cu)
 cudaError_t vec_scale_mul(const double* a, const double* b, double* out, int64_t n, cudaStream_t st);  // out = a*b
+// dst[q] = src[map[q]] (0 where map[q] < 0): a matrix's values into its sliced layout
+template <class V>
+cudaError_t sell_gather(const int* map, const V* src, V* dst, int64_t n, int num_sms, cudaStream_t st);
 cudaError_t vec_to_f32(const double* a, float* out, int64_t n, cudaStream_t st);
 cudaError_t vec_add_f32(double* x, const float* e, int64_t n, cudaStream_t st);  // x += e
 cudaError_t vec_to_f32_scaled(const double* a, double scale, float* out, int64_t n, cudaStream_t st);

@@ -55,7 +55,77 @@ struct SpmvView {
     // short rows in processing order (null: index order, non-short rows skipped)
     const int* short_order = nullptr;
     int n_short = 0;
+    // short rows in the sliced layout (items.h, SellHost); n_sell = 0: the
+    // CSR short-row loop instead
+    int n_sell = 0;
+    int sell_W = 1;
+    const int* sell_ptr = nullptr;
+    const int* sell_perm = nullptr;
+    const int* sell_idx = nullptr;
+    const V* sell_val = nullptr;
 };
+
+// Short rows in the sliced layout: one lane per row, a slice of 32 rows per
+// group of W warps of the CTA (warp `sub` of the group takes step blocks
+// sub, sub + W, ...; each step block is kSellStep entries read with one
+// vector load of indices and one of values); the W partial sums of a row
+// are added in warp order through shared memory (red: the CTA's blockDim
+// doubles) by the group's first warp, which runs the epilogue.  One FMA per
+// entry and no shuffle reductions: GB300's FP64 pipe (~2 lanes / clk / SM)
+// is close to the HBM rate of these passes.  Every thread of the CTA must
+// call it (it synchronises the CTA).
+template <class V, class XF, class EP>
+HELP_DEVINL void spmv_sell(const SpmvView<V>& M, const XF& xf, const EP& ep, double* red) {
+    using V2 = typename Vec2<V>::T;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const int W = M.sell_W <= nw ? M.sell_W : nw;
+    const int groups = nw / W, grp = warp / W, sub = warp - grp * W;
+    const int* __restrict__ sidx = M.sell_idx;
+    const V* __restrict__ sval = M.sell_val;
+    constexpr int BS = 32 * kSellStep;  // entries per step block of a slice
+    for (int base = blockIdx.x * groups; base < M.n_sell; base += gridDim.x * groups) {
+        const int s = base + grp;
+        V acc = V(0);
+        if (grp < groups && s < M.n_sell) {
+            const int b = ld_ro(M.sell_ptr + s), e = ld_ro(M.sell_ptr + s + 1);
+            int q = b + sub * BS + lane * kSellStep;
+            for (; q + W * BS < e; q += 2 * W * BS) {
+                const int2 c0 = ld_stream_na(reinterpret_cast<const int2*>(sidx + q));
+                const int2 c1 = ld_stream_na(reinterpret_cast<const int2*>(sidx + q + W * BS));
+                const V2 v0 = ld_stream_na(reinterpret_cast<const V2*>(sval + q));
+                const V2 v1 = ld_stream_na(reinterpret_cast<const V2*>(sval + q + W * BS));
+                const V x0 = xf(c0.x), x1 = xf(c0.y), x2 = xf(c1.x), x3 = xf(c1.y);
+                acc = fma_t(v0.x, x0, acc);
+                acc = fma_t(v0.y, x1, acc);
+                acc = fma_t(v1.x, x2, acc);
+                acc = fma_t(v1.y, x3, acc);
+            }
+            if (q < e) {
+                const int2 c0 = ld_stream_na(reinterpret_cast<const int2*>(sidx + q));
+                const V2 v0 = ld_stream_na(reinterpret_cast<const V2*>(sval + q));
+                const V x0 = xf(c0.x), x1 = xf(c0.y);
+                acc = fma_t(v0.x, x0, acc);
+                acc = fma_t(v0.y, x1, acc);
+            }
+        }
+        if (W == 1) {
+            if (s < M.n_sell) {
+                const int r = ld_ro(M.sell_perm + 32 * s + lane);
+                if (r >= 0) ep(r, acc);
+            }
+            continue;
+        }
+        __syncthreads();  // red is free (previous slice's sums read)
+        red[threadIdx.x] = (double)acc;
+        __syncthreads();
+        if (sub == 0 && grp < groups && s < M.n_sell) {
+            double t = red[threadIdx.x];
+            for (int u = 1; u < W; ++u) t += red[threadIdx.x + 32 * u];
+            const int r = ld_ro(M.sell_perm + 32 * s + lane);
+            if (r >= 0) ep(r, (V)t);
+        }
+    }
+}
 
 //   xf(col)  -> V     value of the dense operand at index `col`
 //   ep(row, sum)      epilogue for one finished row (called by one thread)
@@ -138,6 +208,10 @@ HELP_DEVINL void spmv_rows(const SpmvView<V>& M, const XF& xf, const EP& ep, con
         if (lane == 0) ep(r, acc);
     }
 
+    if (M.n_sell > 0) {
+        spmv_sell(M, xf, ep, red);
+        return;
+    }
     // short rows: G lanes per row, 32 / G rows per warp step
     const int G = M.G, lg = __ffs(G) - 1;
     const int sub = lane & (G - 1), rpw = 32 >> lg;

@@ -2,6 +2,8 @@
 // right-hand side A D^-1 b_1 - b_2 and the back-substitution
 // D^-1 (b_1 - A^T x_2) of UsePCG_CPU.cpp:103-177, the FP64 residual of the
 // refinement loop) and small vector kernels.
+#include <algorithm>
+
 #include "common.cuh"
 #include "kernels.h"
 #include "spmv.cuh"
@@ -33,6 +35,15 @@ __global__ void __launch_bounds__(256) k_spmv(const SpmvView<V> M, const V* __re
             }
         },
         red);
+}
+
+// B's values into a sliced layout: dst[q] = src[map[q]], 0 on padding
+template <class V>
+__global__ void k_sell_gather(const int* __restrict__ map, const V* __restrict__ src, V* __restrict__ dst, int64_t n) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const int c = map[i];
+        dst[i] = c >= 0 ? ld_ro(src + c) : V(0);
+    }
 }
 
 __global__ void k_mul(const double* __restrict__ a, const double* __restrict__ b, double* __restrict__ out, int64_t n) {
@@ -199,5 +210,16 @@ cudaError_t vec_sumsq(const double* x, int64_t n, double* part, double* out, cud
     k_sum_parts<<<1, 1024, 0, st>>>(part, nb, out);
     return cudaGetLastError();
 }
+
+template <class V>
+cudaError_t sell_gather(const int* map, const V* src, V* dst, int64_t n, int num_sms, cudaStream_t st) {
+    if (n <= 0) return cudaSuccess;
+    const int64_t want = (n + 255) / 256;
+    const int blocks = (int)std::min<int64_t>(want, (int64_t)num_sms * 8);
+    k_sell_gather<V><<<blocks, 256, 0, st>>>(map, src, dst, n);
+    return cudaGetLastError();
+}
+template cudaError_t sell_gather<double>(const int*, const double*, double*, int64_t, int, cudaStream_t);
+template cudaError_t sell_gather<float>(const int*, const float*, float*, int64_t, int, cudaStream_t);
 
 }  // namespace help
