@@ -22,7 +22,9 @@
 // Options come from the environment (defaults = the reference's PCG:
 // 10 pivots, FP64, relative tolerance 1e-20): HELP_GPU_PIVOTS,
 // HELP_GPU_PRECISION (fp64 | mixed), HELP_GPU_CG_TOL, HELP_GPU_CG_MAX_ITER,
-// HELP_GPU_DEVICE.
+// HELP_GPU_DEVICE, HELP_GPU_CAP_OK (1: a solve that stops at the iteration
+// cap hands back its inexact direction instead of failing; the reference's
+// CG has no cap).
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -48,6 +50,7 @@ int LinearEquation_Construct() {
     if (const char* s = std::getenv("HELP_GPU_CG_TOL")) opt.cg_tol = std::atof(s);
     if (const char* s = std::getenv("HELP_GPU_CG_MAX_ITER")) opt.cg_max_iter = std::atoll(s);
     if (const char* s = std::getenv("HELP_GPU_DEVICE")) opt.device = std::atoi(s);
+    if (const char* s = std::getenv("HELP_GPU_CAP_OK")) opt.cap_ok = std::atoi(s);
     help_check(help_pcg_create(&opt, &g_help_ctx), "help_pcg_create");
     // CSC of A from the column lists (rows are sorted inside each column
     // after Presolve_Init, Presolve.cpp:77-113)

@@ -20,8 +20,10 @@
 //     slot and takes a ticket on the row; the CTA that takes the last ticket
 //     adds the row's partials in segment order (deterministic), resets the
 //     ticket and runs the epilogue.  No CTA waits for another.
-// Loads go through L1 (read-only path) so the neighbouring elements a group
-// reads next reuse the sectors already fetched.  All loops are grid-stride
+// Short rows go through the sliced layout where the matrix has one (B = A
+// D^-1/2 of A and A^T), else through L1 (read-only path) so the neighbouring
+// elements a group reads next reuse the sectors already fetched; medium and
+// long rows are read in aligned pairs (range_dot).  All loops are grid-stride
 // over every warp / block of the launch, so the same routine serves the
 // standalone kernels, the CG graph kernels and the single-cluster CG kernel.  One FMA per
 // nonzero and few shuffle adds matter on GB300, whose FP64 rate (~2
@@ -127,6 +129,44 @@ HELP_DEVINL void spmv_sell(const SpmvView<V>& M, const XF& xf, const EP& ep, dou
     }
 }
 
+// Sum over one contiguous range [b, e) of a CSR row by a team of T threads
+// (t = the thread's place in it): entries in aligned pairs, one vector load
+// of indices and one of values per pair, two pairs in flight per thread; the
+// unpaired first and last entries by thread 0.
+template <class V, class XF>
+HELP_DEVINL V range_dot(const int* __restrict__ idx, const V* __restrict__ val, int b, int e, int t, int T,
+                        const XF& xf) {
+    using V2 = typename Vec2<V>::T;
+    V acc = V(0);
+    int q0 = b;
+    if ((q0 & 1) && q0 < e) {
+        if (t == 0) acc = fma_t(ld_ro(val + q0), xf(ld_ro(idx + q0)), acc);
+        ++q0;
+    }
+    const int np = (e - q0) >> 1;
+    const int2* __restrict__ ip = reinterpret_cast<const int2*>(idx + q0);
+    const V2* __restrict__ vp = reinterpret_cast<const V2*>(val + q0);
+    int p = t;
+    for (; p + T < np; p += 2 * T) {
+        const int2 c0 = ld_stream_na(ip + p), c1 = ld_stream_na(ip + p + T);
+        const V2 v0 = ld_stream_na(vp + p), v1 = ld_stream_na(vp + p + T);
+        const V x0 = xf(c0.x), x1 = xf(c0.y), x2 = xf(c1.x), x3 = xf(c1.y);
+        acc = fma_t(v0.x, x0, acc);
+        acc = fma_t(v0.y, x1, acc);
+        acc = fma_t(v1.x, x2, acc);
+        acc = fma_t(v1.y, x3, acc);
+    }
+    if (p < np) {
+        const int2 c0 = ld_stream_na(ip + p);
+        const V2 v0 = ld_stream_na(vp + p);
+        const V x0 = xf(c0.x), x1 = xf(c0.y);
+        acc = fma_t(v0.x, x0, acc);
+        acc = fma_t(v0.y, x1, acc);
+    }
+    if (((e - q0) & 1) && t == 0) acc = fma_t(ld_ro(val + e - 1), xf(ld_ro(idx + e - 1)), acc);
+    return acc;
+}
+
 //   xf(col)  -> V     value of the dense operand at index `col`
 //   ep(row, sum)      epilogue for one finished row (called by one thread)
 //   epl(row, sum)     the same for long rows; it runs in whichever CTA
@@ -148,20 +188,7 @@ HELP_DEVINL void spmv_rows(const SpmvView<V>& M, const XF& xf, const EP& ep, con
     for (int sg = blockIdx.x; sg < M.n_seg; sg += gridDim.x) {
         const int4 S = ld_ro(M.segs + sg);
         const int r = S.x, b = S.y, e = S.z, j = S.w;
-        V acc = V(0);
-        int q = b + tid;
-        for (; q + 3 * nthr < e; q += 4 * nthr) {
-            const int c0 = ld_ro(idx + q), c1 = ld_ro(idx + q + nthr);
-            const int c2 = ld_ro(idx + q + 2 * nthr), c3 = ld_ro(idx + q + 3 * nthr);
-            const V v0 = ld_ro(val + q), v1 = ld_ro(val + q + nthr);
-            const V v2 = ld_ro(val + q + 2 * nthr), v3 = ld_ro(val + q + 3 * nthr);
-            const V x0 = xf(c0), x1 = xf(c1), x2 = xf(c2), x3 = xf(c3);
-            acc = fma_t(v0, x0, acc);
-            acc = fma_t(v1, x1, acc);
-            acc = fma_t(v2, x2, acc);
-            acc = fma_t(v3, x3, acc);
-        }
-        for (; q < e; q += nthr) acc = fma_t(ld_ro(val + q), xf(ld_ro(idx + q)), acc);
+        const V acc = range_dot<V>(idx, val, b, e, tid, nthr, xf);
         const double sum = block_sum((double)acc, red);
         const int nseg = ld_ro(M.long_nseg + j);
         if (nseg == 1) {
@@ -190,20 +217,7 @@ HELP_DEVINL void spmv_rows(const SpmvView<V>& M, const XF& xf, const EP& ep, con
     for (int i = gw; i < M.n_med; i += tw) {
         const int r = ld_ro(M.med_rows + i);
         const int b = ld_ro(ptr + r), e = ld_ro(ptr + r + 1);
-        V acc = V(0);
-        int q = b + lane;
-        for (; q + 96 < e; q += 128) {
-            const int c0 = ld_ro(idx + q), c1 = ld_ro(idx + q + 32);
-            const int c2 = ld_ro(idx + q + 64), c3 = ld_ro(idx + q + 96);
-            const V v0 = ld_ro(val + q), v1 = ld_ro(val + q + 32);
-            const V v2 = ld_ro(val + q + 64), v3 = ld_ro(val + q + 96);
-            const V x0 = xf(c0), x1 = xf(c1), x2 = xf(c2), x3 = xf(c3);
-            acc = fma_t(v0, x0, acc);
-            acc = fma_t(v1, x1, acc);
-            acc = fma_t(v2, x2, acc);
-            acc = fma_t(v3, x3, acc);
-        }
-        for (; q < e; q += 32) acc = fma_t(ld_ro(val + q), xf(ld_ro(idx + q)), acc);
+        V acc = range_dot<V>(idx, val, b, e, lane, 32, xf);
         acc = warp_sum(acc);
         if (lane == 0) ep(r, acc);
     }
