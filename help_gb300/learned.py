@@ -225,21 +225,24 @@ class _Recorder:
                                 destruct=f(self._fns[3]), matvec=f(self._fns[4]))
 
 
-def collect(lp, pivots: int, cg_tol: float = 1e-10, device: int = 0) -> list[dict]:
+def collect(lp, pivots: int, cg_tol: float = 1e-10, device: int = 0, max_seconds: float = 0.0,
+            cg_max_iter: int = 200_000, cap_ok: bool = False) -> list[dict]:
     """Renews of one IPM run of ``lp`` with the plain PCG (a zero model attached
-    so the solutions of every slot are kept for the next renew's features)."""
+    so the solutions of every slot are kept for the next renew's features);
+    ``max_seconds`` > 0 keeps the renews reached within that time."""
     from . import hsd
 
     zero = Mlp(device, zero_params())
-    with GpuNormalEquations(pivots=pivots, cg_tol=cg_tol, cg_max_iter=200_000, device=device) as ne:
+    with GpuNormalEquations(pivots=pivots, cg_tol=cg_tol, cg_max_iter=cg_max_iter, device=device,
+                            cap_ok=cap_ok) as ne:
         ne._check(ne.lib.help_pcg_attach_mlp(ne.ctx, zero.h))
         rec = _Recorder(ne, lp.m, lp.n)
-        res = hsd.solve_lp(lp, rec.backend())
+        res = hsd.solve_lp(lp, rec.backend(), max_seconds=max_seconds)
         ne._check(ne.lib.help_pcg_attach_mlp(ne.ctx, None))
     zero.close()
     if rec.error is not None:
         raise RuntimeError("recording the IPM run failed: %r" % (rec.error,)) from rec.error
-    if res["rc"] != 0 or res["status"] != 0:
+    if res["rc"] != 0 or res["status"] not in ((0, 2) if max_seconds > 0 else (0,)):
         raise RuntimeError("IPM failed while collecting (rc %d, status %d)" % (res["rc"], res["status"]))
     return rec.renews
 
@@ -316,6 +319,54 @@ def targets(lp, renews: list[dict], dense_max: int = 4000, diag: bool = True) ->
             X.append(cur["feat"][min(s, SLOTS - 1)])
             T.append(t)
             W.append(w)
+    return {"X": np.concatenate(X).astype(np.float32), "T": np.concatenate(T).astype(np.float32),
+            "W": np.concatenate(W).astype(np.float32)}
+
+
+def energy_scale_target_sparse(A, d: np.ndarray, xp: np.ndarray, xc: np.ndarray, ridge: float = 100.0,
+                               tol: float = 1e-8, maxiter: int = 2000) -> np.ndarray:
+    """energy_scale_target with G = A D^-1 A^T applied as two sparse products
+    (A: scipy CSR), for systems too large for a dense G: the ridge system
+    (diag(xp) G diag(xp) + lam I) s = diag(xp) G xc + lam a* solved by
+    Jacobi-preconditioned CG (its diagonal: xp^2 diag(G) + lam)."""
+    from scipy.sparse.linalg import LinearOperator, cg
+
+    dinv = 1.0 / d
+    G = lambda v: A @ (dinv * (A.T @ v))
+    gx = G(xp)
+    den = float(xp @ gx)
+    if not den > 0:
+        return np.ones_like(xp)
+    a = float(xc @ gx) / den
+    dg = np.asarray(A.multiply(A) @ dinv).ravel()
+    diagM = xp * xp * dg
+    lam = ridge * max(float(diagM.mean()), 1e-300)
+    op = LinearOperator((len(xp), len(xp)), matvec=lambda v: xp * G(xp * v) + lam * v, dtype=np.float64)
+    pre = LinearOperator((len(xp), len(xp)), matvec=lambda v: v / (diagM + lam), dtype=np.float64)
+    s, _ = cg(op, xp * G(xc) + lam * a, x0=np.full(len(xp), a), rtol=tol, maxiter=maxiter, M=pre)
+    return s / a if a != 0 else np.ones_like(xp)
+
+
+def targets_sparse(lp, renews: list[dict], ridge: float = 100.0) -> dict:
+    """Training rows of one IPM run with the warm-start head only (output 1,
+    the G-norm-optimal per-row scale, from sparse products); output 0 (the
+    Schur-diagonal head, which needs the dense Schur complement) is given
+    weight 0.  For flows of any size."""
+    from scipy.sparse import csr_matrix
+
+    rp, ci, v = lp.csr()
+    A = csr_matrix((v, ci, rp), shape=(lp.m, lp.n))
+    X, T, W = [], [], []
+    for r in range(1, len(renews)):
+        cur, prev = renews[r], renews[r - 1]
+        for s in range(min(len(cur["x2"]), len(prev["x2"]))):
+            xp, xc = prev["x2"][s], cur["x2"][s]
+            if not (xp @ xp) > 0:
+                continue
+            t1 = np.clip(energy_scale_target_sparse(A, cur["d"], xp, xc, ridge), -4.0, 4.0)
+            X.append(cur["feat"][min(s, SLOTS - 1)])
+            T.append(np.stack([np.zeros(lp.m), t1], 1))
+            W.append(np.stack([np.zeros(lp.m), np.full(lp.m, 1.0 / lp.m)], 1))
     return {"X": np.concatenate(X).astype(np.float32), "T": np.concatenate(T).astype(np.float32),
             "W": np.concatenate(W).astype(np.float32)}
 

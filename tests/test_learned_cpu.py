@@ -53,3 +53,24 @@ def test_feature_bits_round_to_nearest_even():
     z[:, learned.FEATURES:] = 0
     ref = torch.from_numpy(z).to(torch.bfloat16).view(torch.int16).numpy().view(np.uint16)
     assert np.array_equal(bits, ref)
+
+
+def test_sparse_warm_start_target_equals_dense():
+    """The warm-start head's target from sparse products of A equals the one
+    from the dense G = A D^-1 A^T (1e-6 relative: the sparse one is an
+    iterative solve to 1e-8)."""
+    from scipy.sparse import csr_matrix
+
+    from help_gb300 import learned, lp as L
+
+    lp = L.generate(L.spec_mcf(8, 3, 2), 4)
+    rp, ci, v = lp.csr()
+    A = csr_matrix((v, ci, rp), shape=(lp.m, lp.n))
+    rng = np.random.default_rng(0)
+    d = np.exp(rng.uniform(-3, 3, lp.n))
+    xp = rng.standard_normal(lp.m)
+    xc = xp * (1 + 0.1 * rng.standard_normal(lp.m))
+    Ad = learned._dense(lp)
+    t_dense = learned.energy_scale_target((Ad / d) @ Ad.T, xp, xc)
+    t_sparse = learned.energy_scale_target_sparse(A, d, xp, xc)
+    assert np.max(np.abs(t_dense - t_sparse)) <= 1e-6 * np.max(np.abs(t_dense))
