@@ -6,7 +6,9 @@ the 100,000 x 400,000 LP (8 nonzeros per column, 3.2M nonzeros) with d
 log-uniform in [1e-8, 1e8] -- the SpMV GB/s metric -- in FP64 (the drop-in
 precision).  One step = one product = two CSR row-gather passes,
 t = B^T v then y = B t with B = A D^-1/2.  Inputs are resident in HBM; L2 is
-flushed (256 MB write) before every step.  Achieved bandwidth counts the
+flushed before every step (a 256 MB write, then a 256 MB read of a second
+buffer, so the write's dirty lines are written back before the timed span
+rather than during it).  Achieved bandwidth counts the
 algorithmic bytes of each pass (values and indices once, both vectors once).
 
 Also reported on the same line: the FP32 product (mixed precision), the
@@ -42,7 +44,8 @@ import numpy as np  # noqa: E402
 
 METRIC = "SpMV HBM GB/s: (A D^-1 A^T) v, two CSR row-gather passes (IPM time to 1e-8 gap reported alongside)"
 WORKLOAD = "config 1: m=100000 n=400000, 8 nnz/col (3.2M nnz), d log-uniform [1e-8,1e8]"
-L2_NOTE = "flushed before every step (256 MB write)"
+L2_NOTE = ("flushed before every step: 256 MB write, then 256 MB read of a second buffer (the write's "
+           "dirty lines written back before the timed span)")
 
 
 def alg_bytes(m: int, n: int, nnz: int, elem: int) -> dict:
@@ -656,6 +659,13 @@ def main() -> None:
     g.RenewLinearEquation(d)
 
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)  # 256 MB > L2
+    flush_r = torch.zeros(64 * 1024 * 1024, dtype=torch.float32, device=dev)
+
+    def flush_l2():
+        # evict everything with a write, then replace the write's dirty lines
+        # by clean ones, so their write-back does not land in the timed kernel
+        flush.fill_(1.0)
+        flush_r.sum()
     res = {}
     for prec, dt in (("f64", torch.float64), ("f32", torch.float32)):
         x = torch.randn(m, dtype=dt, device=dev)
@@ -664,7 +674,7 @@ def main() -> None:
         fp32 = prec == "f32"
 
         def step(times):
-            flush.fill_(1.0)
+            flush_l2()
             e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
             e0.record()
             g.matvec_dev("BT", x.data_ptr(), t.data_ptr(), fp32=fp32)
@@ -721,7 +731,7 @@ def main() -> None:
         g.matvec("ADAT", xh)
     spans = []
     for _ in range(args.steps):
-        flush.fill_(1.0)
+        flush_l2()
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         g.matvec("ADAT", xh)
