@@ -449,3 +449,55 @@ def evaluate(lp, pivots: int, params: np.ndarray | None, cg_tol: float = 1e-10, 
     if trace:
         out["trace"] = {"columns": ["s", "rel_gap", "primal_infeas", "dual_infeas", "cg_iterations"], "rows": rows}
     return out
+
+
+def scaling_study(grid: int, commodities: int, pairs: int, train_seeds, held_out, pivots: int = 16,
+                  steps: int = 400, device: int = 0, full_size: dict | None = None) -> dict:
+    """The warm-start head trained on the IPM iterates of flows far past the
+    dense-Schur limit (targets from sparse products, targets_sparse), and its
+    effect on held-out seeds: whole-IPM CG iterations and seconds of the
+    plain PCG, of the same warm start without the network (fixed_warm_params)
+    and of the trained network (warm head only).  ``full_size`` (keys grid,
+    commodities, pairs, seed, pivots, seconds) adds the benchmark's full flow
+    run under a wall-clock cap, compared at the last interior-point
+    iteration every arm reached."""
+    from . import lp as L
+
+    spec = dict(grid=grid, commodities=commodities, pairs=pairs)
+    t0 = time.perf_counter()
+    data = []
+    for s in train_seeds:
+        lp = L.generate(L.spec_mcf(**spec), s)
+        data.append(targets_sparse(lp, collect(lp, pivots, device=device)))
+    train_set = {k: np.concatenate([d[k] for d in data]) for k in ("X", "T", "W")}
+    collect_s = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    params, losses = train(train_set, steps=steps, device=device)
+    params = warm_head_only(params)
+    out = {"flow": "%d x %d grid, %d commodities" % (grid, grid, commodities), "pivots": pivots,
+           "train_seeds": list(train_seeds), "train_rows": int(train_set["X"].shape[0]),
+           "collect_s": round(collect_s, 1), "train_s": round(time.perf_counter() - t0, 2),
+           "loss_first": losses[0], "loss_last": losses[-1], "held_out": []}
+    arms = (("plain", None), ("fixed_warm_start", fixed_warm_params()), ("learned", params))
+    for s in held_out:
+        lp = L.generate(L.spec_mcf(**spec), s)
+        row = {"seed": s, "m": lp.m, "n": lp.n}
+        for name, prm in arms:
+            r = evaluate(lp, pivots, prm, device=device)
+            row[name] = {"cg": r["cg_iterations"], "s": round(r["seconds"], 3), "status": r["status"],
+                         "iterations": r["iterations"], "primal_obj": r["primal_obj"]}
+        out["held_out"].append(row)
+    if full_size:
+        fs = dict(full_size)
+        lp = L.generate(L.spec_mcf(fs["grid"], fs["commodities"], fs["pairs"]), fs["seed"])
+        runs = {name: evaluate(lp, fs["pivots"], prm, device=device, max_seconds=fs["seconds"], cg_tol=1e-8,
+                               cg_max_iter=50_000, cap_ok=True, trace=True) for name, prm in arms}
+        last = min(len(r["trace"]["rows"]) for r in runs.values())
+        out["full_size"] = {"flow": "%d x %d grid, %d commodities, seed %d (m=%d, n=%d)" % (
+            fs["grid"], fs["grid"], fs["commodities"], fs["seed"], lp.m, lp.n), "pivots": fs["pivots"],
+            "cap_s": fs["seconds"], "compared_at_iteration": last - 1}
+        for name, r in runs.items():
+            row = r["trace"]["rows"][last - 1]
+            out["full_size"][name] = {"s": row[0], "rel_gap": row[1], "cg": row[4],
+                                      "iterations_reached": r["iterations"], "final_rel_gap": r["rel_gap"]}
+    return out
