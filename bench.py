@@ -168,8 +168,8 @@ def ipm_run(config: int, precision: str, pivots: int | None = None, lp=None, cg_
     backend, with the FP64 residual ||rhs - G x_2|| / ||rhs|| of every Newton
     solve read back after the solve.  oracle: every Newton system of the run
     (d, b_1, b_2 and the solution) is recorded, and after the timed run each
-    is solved again by the FP64 direct form (pivots = m: the full Cholesky of
-    A D^-1 A^T, CG to 1e-14) to report the solutions' errors against it."""
+    is solved again on the host in FP64 (cpu_fp64_newton_errors) to report
+    the solutions' errors against it."""
     import ctypes as C
 
     from help_gb300 import backend, hsd, native, lp as L
@@ -213,21 +213,7 @@ def ipm_run(config: int, precision: str, pivots: int | None = None, lp=None, cg_
         st = g.stats()
     errs = None
     if oracle and recorded:
-        ex, ey = [], []
-        with backend.GpuNormalEquations(pivots=lp.m, cg_tol=1e-14, cg_max_iter=1000) as o:
-            o.LinearEquation_Construct(lp)
-            last_d = None
-            for d, b1, b2, x1, x2 in recorded:
-                if last_d is None or not np.array_equal(d, last_d):
-                    o.RenewLinearEquation(d)
-                    last_d = d
-                ox1, ox2 = o.SolveLinearEquation(d, b1, b2)
-                ex.append(float(np.linalg.norm(x1 - ox1) / max(np.linalg.norm(ox1), 1e-300)))
-                ey.append(float(np.linalg.norm(x2 - ox2) / max(np.linalg.norm(ox2), 1e-300)))
-        errs = {"oracle": "FP64 direct form (pivots = m, full Cholesky of A D^-1 A^T, CG to 1e-14) on the "
-                          "recorded systems, after the timed run",
-                "dy_rel_err_max": max(ey), "dy_rel_err_median": float(np.median(ey)),
-                "dx_rel_err_max": max(ex), "dx_rel_err_median": float(np.median(ex))}
+        errs = cpu_fp64_newton_errors(lp, recorded)
     res = np.array([s_[0] for s_ in solves]) if solves else np.zeros(1)
     return {"config": "%s: m=%d n=%d nnz=%d" % (name or "config %d" % config, lp.m, lp.n, lp.nnz),
             "form": "%s PCG, k=%d, tol 1e-10, CG path %s" % (
@@ -241,6 +227,42 @@ def ipm_run(config: int, precision: str, pivots: int | None = None, lp=None, cg_
             "newton_residual_max": float(res.max()), "newton_residual_median": float(np.median(res)),
             "backend_seconds": round(r["backend_s"], 3),
             **({"newton_solution_errors": errs} if errs else {})}
+
+
+def cpu_fp64_newton_errors(lp, recorded) -> dict:
+    """Each recorded Newton system [D A^T; A 0][x1; x2] = [b1; b2] solved
+    again on the host, independently of the GPU library: dense
+    G = A D^-1 A^T, LAPACK Cholesky (scipy; where G is not
+    numerically positive definite: LU), one step of iterative refinement, then
+    x1 = D^-1 (b1 - A^T x2) (UsePCG_CPU.cpp:103-177's reduction).  Returns
+    the relative errors of the GPU's x1, x2 against it."""
+    import scipy.linalg as sl
+
+    A = np.zeros((lp.m, lp.n))
+    for j in range(lp.n):
+        A[lp.row_ind[lp.col_ptr[j]:lp.col_ptr[j + 1]], j] = lp.val[lp.col_ptr[j]:lp.col_ptr[j + 1]]
+    ex, ey, n_lu = [], [], 0
+    last_d, fac = None, None
+    for d, b1, b2, x1, x2 in recorded:
+        if last_d is None or not np.array_equal(d, last_d):
+            G = (A / d) @ A.T
+            try:
+                fac = ("chol", sl.cho_factor(G, lower=True))
+            except np.linalg.LinAlgError:
+                fac = ("lu", sl.lu_factor(G))
+                n_lu += 1
+            last_d = d
+        solve = (lambda r: sl.cho_solve(fac[1], r)) if fac[0] == "chol" else (lambda r: sl.lu_solve(fac[1], r))
+        rhs = A @ (b1 / d) - b2
+        ox2 = solve(rhs)
+        ox2 += solve(rhs - G @ ox2)
+        ox1 = (b1 - A.T @ ox2) / d
+        ex.append(float(np.linalg.norm(x1 - ox1) / max(np.linalg.norm(ox1), 1e-300)))
+        ey.append(float(np.linalg.norm(x2 - ox2) / max(np.linalg.norm(ox2), 1e-300)))
+    return {"oracle": "host FP64: dense A D^-1 A^T, LAPACK Cholesky (scipy; LU where not positive definite: %d "
+                      "renews), one refinement step; independent of the GPU library" % n_lu,
+            "dy_rel_err_max": max(ey), "dy_rel_err_median": float(np.median(ey)),
+            "dx_rel_err_max": max(ex), "dx_rel_err_median": float(np.median(ex))}
 
 
 def ipm_time(config: int = 0) -> dict:
