@@ -65,6 +65,21 @@ def peaks() -> dict:
     return {"hbm_gbs": 6800.0, "source": "fallback"}
 
 
+def gather_bound(nnz: int, pass_ms: float, dev, clocks: dict | None) -> dict:
+    """The pass's practical bound for random sparsity: each nonzero gathers an
+    entry of a vector that L1 does not hold, i.e. one L1 -> L2 request, and
+    an SM's L1 issues at most one such request per clock (profiles/
+    spmv_adat_config1.md: that interface is the busiest unit).  bound_us =
+    nnz / (SMs x SM clock); frac = bound / measured pass time."""
+    import torch
+
+    sms = torch.cuda.get_device_properties(dev).multi_processor_count
+    mhz = (clocks or {}).get("sm_mhz") or 2070.0
+    bound_us = nnz / (sms * mhz * 1e6) * 1e6
+    return {"requests": int(nnz), "sms": sms, "sm_mhz": mhz, "bound_us": round(bound_us, 2),
+            "measured_us": round(pass_ms * 1e3, 2), "frac": round(bound_us / (pass_ms * 1e3), 3)}
+
+
 def ncu_traffic() -> dict | None:
     p = os.path.join(ROOT, "profiles", "spmv_adat_config1_traffic.json")
     if os.path.exists(p):
@@ -327,7 +342,9 @@ def spmv_large(steps: int, warmup: int, local: int) -> dict:
             out[prec] = {"value": round(ab["step"] / ((bt + bb) * 1e-3) / 1e9, 1), "unit": "GB/s",
                          "ms_per_step": round(bt + bb, 4),
                          "passes_gbs": {"BT": round(ab["BT"] / (bt * 1e-3) / 1e9, 1),
-                                        "B": round(ab["B"] / (bb * 1e-3) / 1e9, 1)}}
+                                        "B": round(ab["B"] / (bb * 1e-3) / 1e9, 1)},
+                         "gather_bound": {"BT": gather_bound(nnz, bt, dev, None),
+                                          "B": gather_bound(nnz, bb, dev, None)}}
         # the HSD driver's own products (dest += sign A v, dest += sign A^T y)
         # on the device copy of A, host buffers in and out (help_pcg_matvec_acc)
         from help_gb300 import native
@@ -743,7 +760,8 @@ def main() -> None:
     roof = {"bound": "hbm", "kernel": "k_spmv<double> pass %s (%s)" % (dom, "y = B t" if dom == "B" else "t = B^T v"),
             "achieved": round(achieved, 1), "peak": pk["hbm_gbs"], "peak_source": pk["source"], "unit": "GB/s",
             "frac": round(achieved / pk["hbm_gbs"], 4), "algorithmic_bytes": ab64[dom],
-            "traffic": (tr or {}).get(dom), "traffic_source": (tr or {}).get("source")}
+            "traffic": (tr or {}).get(dom), "traffic_source": (tr or {}).get("source"),
+            "gather_bound": gather_bound(nnz, dom_ms, dev, res["f64"]["clocks"])}
 
     # end to end through the C ABI with host buffers (H2D v, D2H y every step)
     # (help_pcg_matvec: the host vector in, the product out, synchronous); L2
