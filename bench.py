@@ -18,7 +18,7 @@ core), the IPM time to a 1e-8 relative gap on the 2,000 x 6,000 LP (GPU,
 plain FP64 PCG, the mixed form against it with the FP64 residual of every
 Newton solve, and the direct form with every row a pivot), the learned
 part's ablation on held-out multicommodity-flow
-LPs, PCG iterations per second (configs 0 and 1 by default), the same
+LPs, PCG iterations per second (configs 0, 1 and 4 by default), the same
 product on the 104M-nonzero block-angular LP, the live
 roofline of the dominant kernel and the SM clocks sampled during the timed
 region.
@@ -656,7 +656,7 @@ def main() -> None:
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-ipm", action="store_true", help="skip the IPM-time and learned-part measurements")
     ap.add_argument("--no-large", action="store_true", help="skip the 104M-nonzero SpMV measurement")
-    ap.add_argument("--pcg-configs", default="0,1", help="configurations whose PCG iteration rate is measured")
+    ap.add_argument("--pcg-configs", default="0,1,4", help="configurations whose PCG iteration rate is measured")
     ap.add_argument("--pcg-iters", type=int, default=500, help="CG iterations per rate measurement")
     ap.add_argument("--pcg-only", action="store_true", help="only the PCG iteration rates (profiling runs)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baselines beyond the product loop")
