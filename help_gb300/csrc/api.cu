@@ -109,10 +109,10 @@ int upload_split(help_pcg* ctx, RowSplit& S, const int32_t* ptr, int32_t rows, i
 // idx (host column indices, may be null): also lay the short rows out in
 // slices for B's products (A and A^T, whose B values are refreshed at renew)
 int upload_plan(help_pcg* ctx, RowPlan& P, const int32_t* ptr, int32_t rows, bool with_f32,
-                const int32_t* idx = nullptr) {
+                const int32_t* idx = nullptr, int per_lane64 = kPerLaneF64, int per_lane32 = kPerLaneF32) {
     P.rows = rows;
-    int rc = upload_split(ctx, P.s64, ptr, rows, kGminF64, kPerLaneF64, idx, 8);
-    if (!rc && with_f32) rc = upload_split(ctx, P.s32, ptr, rows, kGminF32, kPerLaneF32, idx, 4);
+    int rc = upload_split(ctx, P.s64, ptr, rows, kGminF64, per_lane64, idx, 8);
+    if (!rc && with_f32) rc = upload_split(ctx, P.s32, ptr, rows, kGminF32, per_lane32, idx, 4);
     return rc;
 }
 
@@ -758,7 +758,7 @@ int renew_impl(help_pcg* ctx, const double* d_host) {
     ctx->h_tmp.resize((size_t)m + 1);
     CK(cudaMemcpyAsync(ctx->h_tmp.data(), ctx->c_rp.p, 4 * ((size_t)m + 1), cudaMemcpyDeviceToHost, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
-    rc = upload_plan(ctx, ctx->pl_c, ctx->h_tmp.data(), m, mixed);
+    rc = upload_plan(ctx, ctx->pl_c, ctx->h_tmp.data(), m, mixed, nullptr, kPerLaneCF64, kPerLaneCF32);
     if (rc) return rc;
     std::vector<int32_t> ctp((size_t)k + 1, 0);
     if (k > 0) {

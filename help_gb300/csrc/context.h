@@ -66,6 +66,12 @@ constexpr int kGminF64 = 2;
 constexpr int kPerLaneF64 = 7;
 constexpr int kGminF32 = 2;
 constexpr int kPerLaneF32 = 4;
+// C = G[N, P] gathers a, a k-vector that sits in shared memory or L1, so its
+// pass is bound by the FP64 pipe rather than by L2 requests: more nonzeros
+// per lane, fewer shuffle adds and idle lanes per row (config 4's C: rows of
+// ~85 entries, 16 -> 4 lanes each).
+constexpr int kPerLaneCF64 = 24;
+constexpr int kPerLaneCF32 = 16;
 
 constexpr int kTopkBins = 256;
 constexpr int kGraphIters = 8;    // CG iterations per graph launch

@@ -420,12 +420,24 @@ __global__ void k_schur_diag(const int* __restrict__ c_rp, const int* __restrict
             continue;
         }
         const int b = c_rp[i], e = c_rp[i + 1];
+        // c^T W c with W symmetric: sum over entries a of
+        // c_a (W_aa c_a + 2 sum_{b > a} W_ab c_b), half the W reads; a lane
+        // takes entry p and its mirror len-1-p, so every lane walks len - 1
+        // entries of the triangle
+        const int len = e - b, half = (len + 1) >> 1;
         double qf = 0.0;
-        for (int ea = b + lane; ea < e; ea += 32) {
-            const double* Wr = W + (size_t)c_ci[ea] * k;
+        auto term = [&](int ea) {
+            const int a = c_ci[ea];
+            const double ca = c_v[ea];
+            const double* Wr = W + (size_t)a * k;
             double acc = 0.0;
-            for (int eb = b; eb < e; ++eb) acc = fma(__ldg(Wr + c_ci[eb]), c_v[eb], acc);
-            qf = fma(c_v[ea], acc, qf);
+            for (int eb = ea + 1; eb < e; ++eb) acc = fma(__ldg(Wr + c_ci[eb]), c_v[eb], acc);
+            return ca * fma(__ldg(Wr + a), ca, 2.0 * acc);
+        };
+        for (int p = lane; p < half; p += 32) {
+            qf += term(b + p);
+            const int q = len - 1 - p;
+            if (q > p) qf += term(b + q);
         }
         qf = warp_sum(qf);
         if (lane == 0) {
