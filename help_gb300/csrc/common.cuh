@@ -30,48 +30,22 @@ HELP_DEVINL T ld_ro(const T* p) {
 }
 
 // Streamed once per kernel (a matrix's indices and values): non-coherent
-// path without allocating in L1, so L1 keeps the gathered vector's lines, and
-// first in line for eviction from L2 (`pol` from l2_evict_first()), so the
-// matrix streaming through L2 does not push out the vector the pass gathers
-// from (config 4: a 64 MB vector beside a 1.25 GB matrix stream).
-HELP_DEVINL unsigned long long l2_evict_first() {
-    unsigned long long pol;
-    asm("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(pol));
-    return pol;
-}
-HELP_DEVINL int2 ld_stream_na(const int2* p, unsigned long long pol) {
+// path without allocating in L1, so L1 keeps the gathered vector's lines.
+HELP_DEVINL int2 ld_stream_na(const int2* p) {
     int2 v;
-    asm("ld.global.nc.L1::no_allocate.L2::cache_hint.v2.s32 {%0,%1}, [%2], %3;" : "=r"(v.x), "=r"(v.y) : "l"(p), "l"(pol));
+    asm("ld.global.nc.L1::no_allocate.v2.s32 {%0,%1}, [%2];" : "=r"(v.x), "=r"(v.y) : "l"(p));
     return v;
 }
-HELP_DEVINL double2 ld_stream_na(const double2* p, unsigned long long pol) {
+HELP_DEVINL double2 ld_stream_na(const double2* p) {
     double2 v;
-    asm("ld.global.nc.L1::no_allocate.L2::cache_hint.v2.f64 {%0,%1}, [%2], %3;" : "=d"(v.x), "=d"(v.y) : "l"(p), "l"(pol));
+    asm("ld.global.nc.L1::no_allocate.v2.f64 {%0,%1}, [%2];" : "=d"(v.x), "=d"(v.y) : "l"(p));
     return v;
 }
-HELP_DEVINL float2 ld_stream_na(const float2* p, unsigned long long pol) {
+HELP_DEVINL float2 ld_stream_na(const float2* p) {
     float2 v;
-    asm("ld.global.nc.L1::no_allocate.L2::cache_hint.v2.f32 {%0,%1}, [%2], %3;" : "=f"(v.x), "=f"(v.y) : "l"(p), "l"(pol));
+    asm("ld.global.nc.L1::no_allocate.v2.f32 {%0,%1}, [%2];" : "=f"(v.x), "=f"(v.y) : "l"(p));
     return v;
 }
-// The same hint for scalar loads that keep L1 allocation (the CSR short-row
-// loop, where a lane group's next loads reuse the sectors just fetched).
-HELP_DEVINL int ld_ro_evict(const int* p, unsigned long long pol) {
-    int v;
-    asm("ld.global.nc.L2::cache_hint.s32 %0, [%1], %2;" : "=r"(v) : "l"(p), "l"(pol));
-    return v;
-}
-HELP_DEVINL double ld_ro_evict(const double* p, unsigned long long pol) {
-    double v;
-    asm("ld.global.nc.L2::cache_hint.f64 %0, [%1], %2;" : "=d"(v) : "l"(p), "l"(pol));
-    return v;
-}
-HELP_DEVINL float ld_ro_evict(const float* p, unsigned long long pol) {
-    float v;
-    asm("ld.global.nc.L2::cache_hint.f32 %0, [%1], %2;" : "=f"(v) : "l"(p), "l"(pol));
-    return v;
-}
-
 template <class V>
 struct Vec2;
 template <>

@@ -79,7 +79,6 @@ struct SpmvView {
 template <class V, class XF, class EP>
 HELP_DEVINL void spmv_sell(const SpmvView<V>& M, const XF& xf, const EP& ep, double* red) {
     using V2 = typename Vec2<V>::T;
-    const unsigned long long pol = l2_evict_first();
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     const int W = M.sell_W <= nw ? M.sell_W : nw;
     const int groups = nw / W, grp = warp / W, sub = warp - grp * W;
@@ -93,10 +92,10 @@ HELP_DEVINL void spmv_sell(const SpmvView<V>& M, const XF& xf, const EP& ep, dou
             const int b = ld_ro(M.sell_ptr + s), e = ld_ro(M.sell_ptr + s + 1);
             int q = b + sub * BS + lane * kSellStep;
             for (; q + W * BS < e; q += 2 * W * BS) {
-                const int2 c0 = ld_stream_na(reinterpret_cast<const int2*>(sidx + q), pol);
-                const int2 c1 = ld_stream_na(reinterpret_cast<const int2*>(sidx + q + W * BS), pol);
-                const V2 v0 = ld_stream_na(reinterpret_cast<const V2*>(sval + q), pol);
-                const V2 v1 = ld_stream_na(reinterpret_cast<const V2*>(sval + q + W * BS), pol);
+                const int2 c0 = ld_stream_na(reinterpret_cast<const int2*>(sidx + q));
+                const int2 c1 = ld_stream_na(reinterpret_cast<const int2*>(sidx + q + W * BS));
+                const V2 v0 = ld_stream_na(reinterpret_cast<const V2*>(sval + q));
+                const V2 v1 = ld_stream_na(reinterpret_cast<const V2*>(sval + q + W * BS));
                 const V x0 = xf(c0.x), x1 = xf(c0.y), x2 = xf(c1.x), x3 = xf(c1.y);
                 acc = fma_t(v0.x, x0, acc);
                 acc = fma_t(v0.y, x1, acc);
@@ -104,8 +103,8 @@ HELP_DEVINL void spmv_sell(const SpmvView<V>& M, const XF& xf, const EP& ep, dou
                 acc = fma_t(v1.y, x3, acc);
             }
             if (q < e) {
-                const int2 c0 = ld_stream_na(reinterpret_cast<const int2*>(sidx + q), pol);
-                const V2 v0 = ld_stream_na(reinterpret_cast<const V2*>(sval + q), pol);
+                const int2 c0 = ld_stream_na(reinterpret_cast<const int2*>(sidx + q));
+                const V2 v0 = ld_stream_na(reinterpret_cast<const V2*>(sval + q));
                 const V x0 = xf(c0.x), x1 = xf(c0.y);
                 acc = fma_t(v0.x, x0, acc);
                 acc = fma_t(v0.y, x1, acc);
@@ -138,7 +137,6 @@ template <class V, class XF>
 HELP_DEVINL V range_dot(const int* __restrict__ idx, const V* __restrict__ val, int b, int e, int t, int T,
                         const XF& xf) {
     using V2 = typename Vec2<V>::T;
-    const unsigned long long pol = l2_evict_first();
     V acc = V(0);
     int q0 = b;
     if ((q0 & 1) && q0 < e) {
@@ -150,8 +148,8 @@ HELP_DEVINL V range_dot(const int* __restrict__ idx, const V* __restrict__ val, 
     const V2* __restrict__ vp = reinterpret_cast<const V2*>(val + q0);
     int p = t;
     for (; p + T < np; p += 2 * T) {
-        const int2 c0 = ld_stream_na(ip + p, pol), c1 = ld_stream_na(ip + p + T, pol);
-        const V2 v0 = ld_stream_na(vp + p, pol), v1 = ld_stream_na(vp + p + T, pol);
+        const int2 c0 = ld_stream_na(ip + p), c1 = ld_stream_na(ip + p + T);
+        const V2 v0 = ld_stream_na(vp + p), v1 = ld_stream_na(vp + p + T);
         const V x0 = xf(c0.x), x1 = xf(c0.y), x2 = xf(c1.x), x3 = xf(c1.y);
         acc = fma_t(v0.x, x0, acc);
         acc = fma_t(v0.y, x1, acc);
@@ -159,8 +157,8 @@ HELP_DEVINL V range_dot(const int* __restrict__ idx, const V* __restrict__ val, 
         acc = fma_t(v1.y, x3, acc);
     }
     if (p < np) {
-        const int2 c0 = ld_stream_na(ip + p, pol);
-        const V2 v0 = ld_stream_na(vp + p, pol);
+        const int2 c0 = ld_stream_na(ip + p);
+        const V2 v0 = ld_stream_na(vp + p);
         const V x0 = xf(c0.x), x1 = xf(c0.y);
         acc = fma_t(v0.x, x0, acc);
         acc = fma_t(v0.y, x1, acc);
@@ -245,19 +243,18 @@ HELP_DEVINL void spmv_rows(const SpmvView<V>& M, const XF& xf, const EP& ep, con
         if (!mine) e = b;
         V acc = V(0);
         int q = b + sub;
-        const unsigned long long pol = l2_evict_first();
         for (; q + 3 * G < e; q += 4 * G) {
-            const int c0 = ld_ro_evict(idx + q, pol), c1 = ld_ro_evict(idx + q + G, pol);
-            const int c2 = ld_ro_evict(idx + q + 2 * G, pol), c3 = ld_ro_evict(idx + q + 3 * G, pol);
-            const V v0 = ld_ro_evict(val + q, pol), v1 = ld_ro_evict(val + q + G, pol);
-            const V v2 = ld_ro_evict(val + q + 2 * G, pol), v3 = ld_ro_evict(val + q + 3 * G, pol);
+            const int c0 = ld_ro(idx + q), c1 = ld_ro(idx + q + G);
+            const int c2 = ld_ro(idx + q + 2 * G), c3 = ld_ro(idx + q + 3 * G);
+            const V v0 = ld_ro(val + q), v1 = ld_ro(val + q + G);
+            const V v2 = ld_ro(val + q + 2 * G), v3 = ld_ro(val + q + 3 * G);
             const V x0 = xf(c0), x1 = xf(c1), x2 = xf(c2), x3 = xf(c3);
             acc = fma_t(v0, x0, acc);
             acc = fma_t(v1, x1, acc);
             acc = fma_t(v2, x2, acc);
             acc = fma_t(v3, x3, acc);
         }
-        for (; q < e; q += G) acc = fma_t(ld_ro_evict(val + q, pol), xf(ld_ro_evict(idx + q, pol)), acc);
+        for (; q < e; q += G) acc = fma_t(ld_ro(val + q), xf(ld_ro(idx + q)), acc);
         for (int o = G >> 1; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
         if (mine && sub == 0) ep(r, acc);
     }
