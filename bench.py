@@ -485,6 +485,9 @@ def start_cpu_ipm():
     p = ctx.Process(target=_cpu_ipm_worker, args=(child, core), daemon=True)
     p.start()
     child.close()
+    if core is not None:
+        # keep this process (and the CPU baselines it times) off that core
+        os.sched_setaffinity(0, set(cores) - {core})
     return p, parent
 
 
