@@ -74,6 +74,7 @@ struct Hsd {
     std::vector<double> hat_r_xz, dx, dy, dz, dx_b, dy_b, dz_b;
     double hat_r_tk = 0, dtau = 0, dkappa = 0;
     std::vector<double> Dir_p, Dir_q, Dir_u, Dir_v, Dir_RHS1, Dir_RHS2, SLE_RHS1, SLE_RHS2, LEBOT_RHS1, LEBOT_RHS2;
+    std::vector<double> masked;  // hrxz where x < z, for the device product
     double backend_s = 0;
     int solves = 0, renews = 0;
     int be_error = 0;
@@ -198,11 +199,20 @@ struct Hsd {
         for (int i = 0; i < n; i++) hrxz[i] /= std::max(x[i], z[i]);
         for (int i = 0; i < n; i++)
             if (x[i] >= z[i]) Dir_RHS1[i] += hrxz[i];
-        for (int i = 0; i < n; i++)
-            if (x[i] < z[i]) {
-                for (int j = lp->col_ptr[i]; j < lp->col_ptr[i + 1]; j++)
-                    Dir_RHS2[lp->row_ind[j]] -= lp->val[j] * hrxz[i];
-            }
+        if (be->matvec) {
+            // the same product, A (hrxz where x < z), on the backend's copy
+            // of A: a scatter over every nonzero on the host otherwise (the
+            // driver's largest host cost at 10^8 nonzeros); row sums in the
+            // device's order, as for the driver's other products
+            for (int i = 0; i < n; i++) masked[i] = (x[i] < z[i]) ? hrxz[i] : 0.0;
+            ATimes(0, -1, masked.data(), Dir_RHS2.data());
+        } else {
+            for (int i = 0; i < n; i++)
+                if (x[i] < z[i]) {
+                    for (int j = lp->col_ptr[i]; j < lp->col_ptr[i + 1]; j++)
+                        Dir_RHS2[lp->row_ind[j]] -= lp->val[j] * hrxz[i];
+                }
+        }
         double UP = eta * r_g + hrtk / tau;
         for (int i = 0; i < n; i++)
             if (x[i] < z[i]) UP += c[i] * hrxz[i];
@@ -486,6 +496,7 @@ static int hsd_solve(const help_lp* lp, const help_ne_backend* be, const help_hs
     for (auto* v : {&h.x, &h.z, &h.D, &h.r_d, &h.hat_r_xz, &h.dx, &h.dz, &h.dx_b, &h.dz_b, &h.Dir_p, &h.Dir_u,
                     &h.Dir_RHS1, &h.SLE_RHS1, &h.LEBOT_RHS1})
         v->assign(n, 0.0);
+    if (be->matvec) h.masked.assign(n, 0.0);
     for (auto* v : {&h.y, &h.r_p, &h.dy, &h.dy_b, &h.Dir_q, &h.Dir_v, &h.Dir_RHS2, &h.SLE_RHS2, &h.LEBOT_RHS2})
         v->assign(m, 0.0);
     double tb = now_s();
