@@ -51,8 +51,12 @@ HELP_DEVINL double sum_parts(const double* p, const double* p2, int nb, double* 
 }
 
 // Writes this block's partial and returns true in the last block to finish.
+// The barrier first: the ticket announces every write of the block (k_p3's
+// w entries come from any of its warps), so no thread may still be writing
+// when thread 0 fences and takes it.
 HELP_DEVINL bool publish_partial(double v, double* part, unsigned int* ticket) {
     __shared__ int s_last;
+    __syncthreads();
     if (threadIdx.x == 0) {
         part[blockIdx.x] = v;
         __threadfence();
