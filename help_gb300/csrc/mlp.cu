@@ -22,6 +22,8 @@
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include "../../include/help_gpu.h"
 #include "common.cuh"
 #include "kernels.h"
@@ -137,6 +139,248 @@ __global__ void __launch_bounds__(kMlpThreads) k_mlp_fwd(const __nv_bfloat16* __
             }
         }
     }
+}
+
+// ---- inference forward on the 5th-generation tensor cores (tcgen05 + TMEM)
+//
+// One CTA of 4 warps takes tiles of 128 rows: the tile's features and the
+// weights sit in shared memory in the canonical K-major layout without
+// swizzle (core matrices of 8 rows x 16 bytes; LBO = 128 bytes between core
+// matrices along K, SBO = (K / 8) x 128 bytes between 8-row groups), one
+// thread issues the layer's tcgen05.mma (M = 128, K = 16 per instruction)
+// into a 64-column TMEM accumulator and commits it to an mbarrier; each warp
+// then reads its 32 rows back with tcgen05.ld, adds the bias, applies ReLU,
+// rounds to BF16 (as the mma.sync kernel does) and writes the next layer's
+// A operand.  Every mbarrier wait is bounded: past the bound the tile's
+// outputs are NaN, the CTA waits once more for the MMA in flight and frees
+// its TMEM before returning.
+constexpr int kTcRows = 128;
+constexpr int kTcThreads = 128;
+constexpr int kTcCols = 64;  // TMEM columns per CTA (FP32 accumulators of N = 64)
+constexpr long kTcWaitPolls = 1L << 20;
+
+struct TcSmem {
+    __nv_bfloat16 x[kTcRows * kF];  // layer-1 A: 16 groups x 2 chunks (SBO 256)
+    __nv_bfloat16 h[kTcRows * kH];  // layer-2/3 A: 16 groups x 8 chunks (SBO 1024)
+    __nv_bfloat16 w1[kH * kF];      // layer-1 B: 8 groups x 2 chunks
+    __nv_bfloat16 w2[kH * kH];      // layer-2 B: 8 groups x 8 chunks
+    __nv_bfloat16 w3[16 * kH];      // layer-3 B: 2 groups x 8 chunks, rows >= HELP_MLP_OUT zero
+    float b1[kH], b2[kH], b3[16];
+    unsigned long long mbar;
+    uint32_t tmem;
+};
+
+// byte offset of element (r, k) of an operand with K columns in the canonical layout
+HELP_DEVINL uint32_t canon(int r, int k, int K) {
+    return (uint32_t)((r >> 3) * (K / 8) * 128 + (k >> 3) * 128 + (r & 7) * 16 + (k & 7) * 2);
+}
+
+HELP_DEVINL uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+// shared-memory matrix descriptor: start >> 4, LBO >> 4, SBO >> 4, version 1, no swizzle
+HELP_DEVINL uint64_t tc_desc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+    return (uint64_t)((addr >> 4) & 0x3FFFu) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
+           ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);
+}
+
+// instruction descriptor, kind::f16: D FP32, A and B BF16, both K-major, N, M = 128
+HELP_DEVINL uint32_t tc_idesc(int n) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(kTcRows >> 4) << 24);
+}
+
+HELP_DEVINL void tc_mma(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t idesc, uint32_t accumulate) {
+    asm volatile(
+        "{\n.reg .pred p;\nsetp.ne.u32 p, %4, 0;\n"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(d_tmem),
+        "l"(a), "l"(b), "r"(idesc), "r"(accumulate));
+}
+
+HELP_DEVINL void tc_commit(uint32_t mbar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbar) : "memory");
+}
+
+HELP_DEVINL bool mbar_wait(uint32_t mbar, uint32_t phase) {
+    for (long i = 0; i < kTcWaitPolls; ++i) {
+        uint32_t done;
+        asm volatile(
+            "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
+            : "=r"(done)
+            : "r"(mbar), "r"(phase)
+            : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+
+HELP_DEVINL void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+HELP_DEVINL void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+HELP_DEVINL void proxy_fence() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+// 16 consecutive FP32 columns of this warp's 32 TMEM lanes
+HELP_DEVINL void tc_ld16(uint32_t taddr, float (&v)[16]) {
+    uint32_t r[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int j = 0; j < 16; ++j) v[j] = __uint_as_float(r[j]);
+}
+
+// bias, ReLU, BF16, into row `row` of the next layer's A operand (64 columns)
+HELP_DEVINL void tc_hidden_out(uint32_t taddr, const float* bias, unsigned char* h, int row) {
+#pragma unroll
+    for (int q = 0; q < kH / 16; ++q) {
+        float v[16];
+        tc_ld16(taddr + 16 * q, v);
+        uint32_t p[8];
+#pragma unroll
+        for (int j = 0; j < 8; ++j)
+            p[j] = pack_bf16(fmaxf(v[2 * j] + bias[16 * q + 2 * j], 0.f),
+                             fmaxf(v[2 * j + 1] + bias[16 * q + 2 * j + 1], 0.f));
+        *reinterpret_cast<uint4*>(h + canon(row, 16 * q, kH)) = make_uint4(p[0], p[1], p[2], p[3]);
+        *reinterpret_cast<uint4*>(h + canon(row, 16 * q + 8, kH)) = make_uint4(p[4], p[5], p[6], p[7]);
+    }
+}
+
+__global__ void __launch_bounds__(kTcThreads) k_mlp_fwd_tc(const __nv_bfloat16* __restrict__ X, long long rows,
+                                                            const MlpDevWeights* __restrict__ w,
+                                                            float* __restrict__ out, bool x16) {
+    extern __shared__ __align__(1024) unsigned char tc_raw[];
+    TcSmem& s = *reinterpret_cast<TcSmem*>(tc_raw);
+    unsigned char* sx = reinterpret_cast<unsigned char*>(s.x);
+    unsigned char* sh = reinterpret_cast<unsigned char*>(s.h);
+    unsigned char* sw1 = reinterpret_cast<unsigned char*>(s.w1);
+    unsigned char* sw2 = reinterpret_cast<unsigned char*>(s.w2);
+    unsigned char* sw3 = reinterpret_cast<unsigned char*>(s.w3);
+    const int tid = threadIdx.x, warp = tid >> 5;
+    for (int i = tid; i < kH * kF; i += kTcThreads)
+        *reinterpret_cast<__nv_bfloat16*>(sw1 + canon(i / kF, i % kF, kF)) = w->w1[i];
+    for (int i = tid; i < kH * kH; i += kTcThreads)
+        *reinterpret_cast<__nv_bfloat16*>(sw2 + canon(i / kH, i % kH, kH)) = w->w2[i];
+    for (int i = tid; i < 16 * kH; i += kTcThreads)
+        *reinterpret_cast<__nv_bfloat16*>(sw3 + canon(i / kH, i % kH, kH)) =
+            i < 8 * kH ? w->w3[i] : __float2bfloat16(0.f);
+    for (int i = tid; i < kH; i += kTcThreads) {
+        s.b1[i] = w->b1[i];
+        s.b2[i] = w->b2[i];
+    }
+    if (tid < 16) s.b3[tid] = tid < 8 ? w->b3[tid] : 0.f;
+    const uint32_t mbar = smem_u32(&s.mbar);
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mbar) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&s.tmem)),
+                     "r"(kTcCols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    proxy_fence();
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = s.tmem;
+    const uint32_t trow = tmem + ((uint32_t)(32 * warp) << 16);  // this warp's 32 lanes
+    const uint32_t ax = smem_u32(sx), ah = smem_u32(sh);
+    const uint32_t b1a = smem_u32(sw1), b2a = smem_u32(sw2), b3a = smem_u32(sw3);
+    uint32_t phase = 0;
+    bool ok = true;
+    const long long ntiles = (rows + kTcRows - 1) / kTcRows;
+    for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const long long r = tile * kTcRows + tid;
+        // features of row r (BF16 pairs: 4-byte aligned) into the layer-1 A operand
+        uint4 f0 = make_uint4(0u, 0u, 0u, 0u), f1 = f0;
+        if (ok && r < rows) {
+            if (x16) {  // a row is 32 bytes: two 16-byte loads
+                const uint4* xr = reinterpret_cast<const uint4*>(X + r * kF);
+                f0 = __ldg(xr);
+                f1 = __ldg(xr + 1);
+            } else {
+                const __nv_bfloat16* xr = X + r * kF;
+                f0 = make_uint4(ld32(xr), ld32(xr + 2), ld32(xr + 4), ld32(xr + 6));
+                f1 = make_uint4(ld32(xr + 8), ld32(xr + 10), ld32(xr + 12), ld32(xr + 14));
+            }
+        }
+        *reinterpret_cast<uint4*>(sx + canon(tid, 0, kF)) = f0;
+        *reinterpret_cast<uint4*>(sx + canon(tid, 8, kF)) = f1;
+        proxy_fence();
+        tc_fence_before();
+        __syncthreads();
+        tc_fence_after();
+        // layer 1: K = 16, one instruction
+        if (ok && tid == 0) {
+            tc_mma(tmem, tc_desc(ax, 128, 256), tc_desc(b1a, 128, 256), tc_idesc(kH), 0u);
+            tc_commit(mbar);
+        }
+        if (ok) ok = mbar_wait(mbar, phase);
+        phase ^= 1u;
+        ok = __syncthreads_and(ok);  // tcgen05.ld is warp-collective: one verdict for the CTA
+        tc_fence_after();
+        if (ok) tc_hidden_out(trow, s.b1, sh, tid);
+        proxy_fence();
+        tc_fence_before();
+        __syncthreads();
+        tc_fence_after();
+        ok = __syncthreads_and(ok);
+        // layer 2: K = 64, four instructions of K = 16 (two core matrices each)
+        if (ok && tid == 0) {
+#pragma unroll
+            for (int ks = 0; ks < kH / 16; ++ks)
+                tc_mma(tmem, tc_desc(ah + 256 * ks, 128, 1024), tc_desc(b2a + 256 * ks, 128, 1024), tc_idesc(kH),
+                       ks > 0 ? 1u : 0u);
+            tc_commit(mbar);
+        }
+        if (ok) ok = mbar_wait(mbar, phase);
+        phase ^= 1u;
+        ok = __syncthreads_and(ok);  // tcgen05.ld is warp-collective: one verdict for the CTA
+        tc_fence_after();
+        if (ok) tc_hidden_out(trow, s.b2, sh, tid);
+        proxy_fence();
+        tc_fence_before();
+        __syncthreads();
+        tc_fence_after();
+        ok = __syncthreads_and(ok);
+        // layer 3: N = 16 (two outputs used), K = 64
+        if (ok && tid == 0) {
+#pragma unroll
+            for (int ks = 0; ks < kH / 16; ++ks)
+                tc_mma(tmem, tc_desc(ah + 256 * ks, 128, 1024), tc_desc(b3a + 256 * ks, 128, 1024), tc_idesc(16),
+                       ks > 0 ? 1u : 0u);
+            tc_commit(mbar);
+        }
+        if (ok) ok = mbar_wait(mbar, phase);
+        phase ^= 1u;
+        ok = __syncthreads_and(ok);  // tcgen05.ld is warp-collective: one verdict for the CTA
+        tc_fence_after();
+        float v[16];
+        if (ok) tc_ld16(trow, v);
+        if (r < rows) {
+            out[r * 2] = ok ? v[0] + s.b3[0] : __int_as_float(0x7fc00000);
+            out[r * 2 + 1] = ok ? v[1] + s.b3[1] : __int_as_float(0x7fc00000);
+        }
+        tc_fence_before();
+        __syncthreads();
+        tc_fence_after();
+        ok = __syncthreads_and(ok);
+    }
+    if (!ok) {
+        // an MMA never signalled: give it one more bounded wait before the
+        // accumulator is freed, and mark the CTA's remaining rows
+        if (tid == 0) mbar_wait(mbar, phase ^ 1u);
+        for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+            const long long r = tile * kTcRows + tid;
+            if (r < rows) out[r * 2] = out[r * 2 + 1] = __int_as_float(0x7fc00000);
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTcCols) : "memory");
 }
 
 // ---- weighted squared error: loss partials, G3 = dL/dout
@@ -402,8 +646,17 @@ cudaError_t mlp_forward(const __nv_bfloat16* X, long long rows, const MlpDevWeig
                         __nv_bfloat16* H1, __nv_bfloat16* H2, int num_sms, cudaStream_t st) {
     if (rows <= 0) return cudaSuccess;
     const int nb = mlp_blocks(rows, num_sms);
-    if (H1) k_mlp_fwd<true><<<nb, kMlpThreads, 0, st>>>(X, rows, w, out, H1, H2);
-    else k_mlp_fwd<false><<<nb, kMlpThreads, 0, st>>>(X, rows, w, out, nullptr, nullptr);
+    if (H1) {
+        k_mlp_fwd<true><<<nb, kMlpThreads, 0, st>>>(X, rows, w, out, H1, H2);
+    } else {
+        // inference: the tcgen05 kernel, 128-row tiles, 6 CTAs per SM (the
+        // most its shared memory allows; 6 x 64 TMEM columns of the SM's 512,
+        // so an allocation never waits)
+        const long long tiles = (rows + kTcRows - 1) / kTcRows;
+        const int tb = (int)std::min<long long>(tiles, 6LL * num_sms);
+        const bool x16 = (reinterpret_cast<uintptr_t>(X) & 15u) == 0;
+        k_mlp_fwd_tc<<<tb, kTcThreads, sizeof(TcSmem), st>>>(X, rows, w, out, x16);
+    }
     return cudaGetLastError();
 }
 

@@ -67,6 +67,30 @@ def test_gpu_forward_matches_oracle(rows):
 
 
 @pytest.mark.gpu
+def test_gpu_inference_forward_matches_training_forward():
+    """The inference forward (tcgen05, TMEM accumulators, several 128-row
+    tiles per CTA and a ragged last tile) against the oracle element-wise and
+    against the training forward (mma.sync) through the loss both give."""
+    torch = pytest.importorskip("torch")
+    from help_gb300 import learned
+
+    rows = 300_001
+    x, t, w = _data(rows, 12)
+    p = R.init_params(13)
+    m = learned.Mlp(0, p)
+    xb = torch.from_numpy(learned.bf16_bits(x).view(np.int16)).cuda()
+    out = m.forward(xb, rows).cpu().numpy().astype(np.float64)
+    ref = R.forward(p, x)[0]
+    assert np.isfinite(out).all()
+    assert np.linalg.norm(out - ref) / np.linalg.norm(ref) < 1e-3
+    assert np.abs(out - ref).max() < 2e-2 * np.abs(ref).max()
+    loss_train, _ = m.loss_grad(xb, torch.from_numpy(t).cuda(), torch.from_numpy(w).cuda(), rows)
+    loss_inf = float(np.sum(w * (out - t) ** 2) / np.sum(w))
+    assert abs(loss_inf - loss_train) <= 1e-5 * abs(loss_train), (loss_inf, loss_train)
+    m.close()
+
+
+@pytest.mark.gpu
 @pytest.mark.parametrize("rows", [640, 37])
 def test_gpu_gradient_matches_oracle(rows):
     torch = pytest.importorskip("torch")
