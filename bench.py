@@ -18,13 +18,13 @@ core), the IPM time to a 1e-8 relative gap on the 2,000 x 6,000 LP (GPU,
 plain FP64 PCG, the mixed form against it with the FP64 residual of every
 Newton solve, and the direct form with every row a pivot), the learned
 part's ablation on held-out multicommodity-flow
-LPs, PCG iterations per second (configs 0, 1 and 4 by default), the same
+LPs and its MLP's forward / training rates, PCG iterations per second (configs 0, 1 and 4 by default), the same
 product on the 104M-nonzero block-angular LP, the live
 roofline of the dominant kernel and the SM clocks sampled during the timed
 region.
 
     python bench.py [--steps K] [--warmup W] [--gpus N] [--impl ours|reference] [--no-ipm] [--no-large]
-                    [--pcg-configs 0,1] [--pcg-iters I] [--pcg-only]
+                    [--pcg-configs 0,1] [--pcg-iters I] [--pcg-only] [--mlp-only [--mlp-rows R]]
 """
 from __future__ import annotations
 
@@ -61,8 +61,8 @@ def peaks() -> dict:
     if os.path.exists(p):
         with open(p) as f:
             d = json.load(f)
-        return {"hbm_gbs": d["hbm_gbs"], "source": "measured"}
-    return {"hbm_gbs": 6800.0, "source": "fallback"}
+        return {"hbm_gbs": d["hbm_gbs"], "bf16_tflops": d.get("bf16_tflops", 1900.0), "source": "measured"}
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "source": "fallback"}
 
 
 def gather_bound(nnz: int, pass_ms: float, dev, clocks: dict | None) -> dict:
@@ -560,6 +560,60 @@ def learned_ablation() -> dict:
             "loss_first": losses[0], "loss_last": losses[-1], "held_out": runs}, params
 
 
+def mlp_rate(rows: int, reps: int, local: int) -> dict:
+    """The learned part's MLP (16 -> 64 -> 64 -> 2, BF16 in, FP32 accumulate)
+    on `rows` seeded feature rows: the inference forward the solver runs after
+    each renew (tcgen05, TMEM accumulators; CUDA events on its stream over
+    `reps` launches, inputs resident) and one training step's forward +
+    backward (mma.sync, activations stored; host wall time, synchronised).
+    Algorithmic FLOPs: 2 (16*64 + 64*64 + 64*2) per row."""
+    import torch
+
+    from help_gb300 import learned
+    from help_gb300 import native
+
+    rng = np.random.default_rng(1)
+    x = rng.standard_normal((rows, native.MLP_IN)).astype(np.float32)
+    x[:, 11:] = 0.0
+    t = rng.standard_normal((rows, native.MLP_OUT)).astype(np.float32)
+    m = learned.Mlp(local, learned.init_params(2))
+    try:
+        xb = torch.from_numpy(learned.bf16_bits(x).view(np.int16)).cuda(local)
+        tt, ww = torch.from_numpy(t).cuda(local), torch.ones((rows, native.MLP_OUT), dtype=torch.float32, device=xb.device)
+        out = torch.empty((rows, native.MLP_OUT), dtype=torch.float32, device=xb.device)
+        st = torch.cuda.current_stream()
+        fwd = lambda: m._check(m.lib.help_mlp_forward(m.h, xb.data_ptr(), rows, out.data_ptr(), st.cuda_stream))
+        for _ in range(3):
+            fwd()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        for _ in range(reps):
+            fwd()
+        e1.record(st)
+        torch.cuda.synchronize()
+        fwd_ms = e0.elapsed_time(e1) / reps
+        for _ in range(2):
+            m.loss_grad(xb, tt, ww, rows)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(3):
+            m.loss_grad(xb, tt, ww, rows)
+        torch.cuda.synchronize()
+        lg_ms = (time.perf_counter() - t0) / 3 * 1e3
+    finally:
+        m.close()
+    flops = 2.0 * rows * (native.MLP_IN * native.MLP_HIDDEN + native.MLP_HIDDEN ** 2 + native.MLP_HIDDEN * native.MLP_OUT)
+    pk = peaks()
+    tf = flops / fwd_ms / 1e9
+    return {"rows": rows, "forward_us": round(fwd_ms * 1e3, 2), "forward_rows_per_s": round(rows / fwd_ms * 1e3),
+            "forward_tflops": round(tf, 1), "forward_frac_of_bf16_peak": round(tf / pk["bf16_tflops"], 4),
+            "bf16_peak_source": pk["source"],
+            "forward_gbs": round(rows * (2 * native.MLP_IN + 4 * native.MLP_OUT) / fwd_ms / 1e6, 1),
+            "train_step_ms": round(lg_ms, 3), "forward_kernel": "k_mlp_fwd_tc (tcgen05.mma kind::f16, M=128)",
+            "train_kernels": "k_mlp_fwd<true>, k_mlp_bwd (mma.sync m16n8k16)"}
+
+
 def presolve_time() -> dict:
     """The host dependent-row presolve (help_lp_remove_dependent_rows, one
     thread): the 200 x 200 grid, 8-commodity flow with every node row kept
@@ -665,6 +719,8 @@ def main() -> None:
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baselines beyond the product loop")
     ap.add_argument("--no-ipm-large", action="store_true", help="skip the capped IPM runs on configs 1 and 4")
     ap.add_argument("--ipm-large-caps", default="1:25,4:45", help="config:seconds per arm of the capped IPM runs")
+    ap.add_argument("--mlp-only", action="store_true", help="only the learned part's MLP rates (profiling runs)")
+    ap.add_argument("--mlp-rows", type=int, default=2_000_000, help="feature rows of the MLP rate measurement")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
@@ -676,6 +732,13 @@ def main() -> None:
         torch.cuda.set_device(local)
         out = {c: pcg_rate(int(c), args.pcg_iters, local) for c in args.pcg_configs.split(",") if c}
         print(json.dumps({"pcg": out}), flush=True)
+        return
+    if args.mlp_only:
+        import torch
+
+        ws, rank, local = dist_env()
+        torch.cuda.set_device(local)
+        print(json.dumps({"mlp": mlp_rate(args.mlp_rows, max(1, args.steps), local)}), flush=True)
         return
 
     ws, rank, local = dist_env()
@@ -801,6 +864,10 @@ def main() -> None:
                 extra["learned"], params = learned_ablation()
             except Exception as e:
                 extra["learned"], params = {"error": str(e)}, None
+            try:
+                extra["mlp"] = mlp_rate(args.mlp_rows, 20, local)
+            except Exception as e:
+                extra["mlp"] = {"error": str(e)}
             try:
                 extra["presolve"] = presolve_time()
             except Exception as e:

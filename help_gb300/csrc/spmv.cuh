@@ -75,9 +75,15 @@ struct SpmvView {
 // doubles) by the group's first warp, which runs the epilogue.  One FMA per
 // entry and no shuffle reductions: GB300's FP64 pipe (~2 lanes / clk / SM)
 // is close to the HBM rate of these passes.  Every thread of the CTA must
-// call it (it synchronises the CTA).
-template <class V, class XF, class EP>
+// call it (it synchronises the CTA).  kDepth (2 or 4): step blocks a lane
+// has in flight (4 or 8 gathers); the sum runs over the lane's blocks in the
+// same order either way, so the results are bitwise the same.  4 pays in
+// the standalone pass (32 -> 40 registers, occupancy unchanged: config 1's
+// B pass 23.9 -> 22.5 us), 2 in the CG kernels (their 40 registers would
+// grow to 48 and cost a CTA per SM: config 1's iteration 83 -> 90 us).
+template <class V, int kDepth, class XF, class EP>
 HELP_DEVINL void spmv_sell(const SpmvView<V>& M, const XF& xf, const EP& ep, double* red) {
+    static_assert(kDepth == 2 || kDepth == 4, "step blocks in flight: 2 or 4");
     using V2 = typename Vec2<V>::T;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     const int W = M.sell_W <= nw ? M.sell_W : nw;
@@ -91,7 +97,29 @@ HELP_DEVINL void spmv_sell(const SpmvView<V>& M, const XF& xf, const EP& ep, dou
         if (grp < groups && s < M.n_sell) {
             const int b = ld_ro(M.sell_ptr + s), e = ld_ro(M.sell_ptr + s + 1);
             int q = b + sub * BS + lane * kSellStep;
-            for (; q + W * BS < e; q += 2 * W * BS) {
+            if constexpr (kDepth == 4) {
+                for (; q + 3 * W * BS < e; q += 4 * W * BS) {
+                    const int2 c0 = ld_stream_na(reinterpret_cast<const int2*>(sidx + q));
+                    const int2 c1 = ld_stream_na(reinterpret_cast<const int2*>(sidx + q + W * BS));
+                    const int2 c2 = ld_stream_na(reinterpret_cast<const int2*>(sidx + q + 2 * W * BS));
+                    const int2 c3 = ld_stream_na(reinterpret_cast<const int2*>(sidx + q + 3 * W * BS));
+                    const V x0 = xf(c0.x), x1 = xf(c0.y), x2 = xf(c1.x), x3 = xf(c1.y);
+                    const V x4 = xf(c2.x), x5 = xf(c2.y), x6 = xf(c3.x), x7 = xf(c3.y);
+                    const V2 v0 = ld_stream_na(reinterpret_cast<const V2*>(sval + q));
+                    const V2 v1 = ld_stream_na(reinterpret_cast<const V2*>(sval + q + W * BS));
+                    const V2 v2 = ld_stream_na(reinterpret_cast<const V2*>(sval + q + 2 * W * BS));
+                    const V2 v3 = ld_stream_na(reinterpret_cast<const V2*>(sval + q + 3 * W * BS));
+                    acc = fma_t(v0.x, x0, acc);
+                    acc = fma_t(v0.y, x1, acc);
+                    acc = fma_t(v1.x, x2, acc);
+                    acc = fma_t(v1.y, x3, acc);
+                    acc = fma_t(v2.x, x4, acc);
+                    acc = fma_t(v2.y, x5, acc);
+                    acc = fma_t(v3.x, x6, acc);
+                    acc = fma_t(v3.y, x7, acc);
+                }
+            }
+            for (; q + W * BS < e; q += 2 * W * BS) {  // after the loop above: at most once
                 const int2 c0 = ld_stream_na(reinterpret_cast<const int2*>(sidx + q));
                 const int2 c1 = ld_stream_na(reinterpret_cast<const int2*>(sidx + q + W * BS));
                 const V2 v0 = ld_stream_na(reinterpret_cast<const V2*>(sval + q));
@@ -174,7 +202,7 @@ HELP_DEVINL V range_dot(const int* __restrict__ idx, const V* __restrict__ val, 
 //                     accumulates a reduction passes an epl that only stores
 //                     and adds the long rows' terms in a fixed order itself
 // red: blockDim doubles of shared memory (CTA reductions of long rows).
-template <class V, class XF, class EP, class EPL>
+template <class V, int kDepth = 2, class XF, class EP, class EPL>
 HELP_DEVINL void spmv_rows(const SpmvView<V>& M, const XF& xf, const EP& ep, const EPL& epl, double* red) {
     const int tid = threadIdx.x, nthr = blockDim.x;
     const int lane = tid & 31, warp = tid >> 5, nw = nthr >> 5;
@@ -223,7 +251,7 @@ HELP_DEVINL void spmv_rows(const SpmvView<V>& M, const XF& xf, const EP& ep, con
     }
 
     if (M.n_sell > 0) {
-        spmv_sell(M, xf, ep, red);
+        spmv_sell<V, kDepth>(M, xf, ep, red);
         return;
     }
     // short rows: G lanes per row, 32 / G rows per warp step
@@ -260,9 +288,9 @@ HELP_DEVINL void spmv_rows(const SpmvView<V>& M, const XF& xf, const EP& ep, con
     }
 }
 
-template <class V, class XF, class EP>
+template <class V, int kDepth = 2, class XF, class EP>
 HELP_DEVINL void spmv_rows(const SpmvView<V>& M, const XF& xf, const EP& ep, double* red) {
-    spmv_rows<V>(M, xf, ep, ep, red);
+    spmv_rows<V, kDepth>(M, xf, ep, ep, red);
 }
 
 }  // namespace help

@@ -17,7 +17,7 @@ __global__ void __launch_bounds__(256) k_spmv(const SpmvView<V> M, const V* __re
                                               const V* __restrict__ aux, const V* __restrict__ aux2,
                                               const double* __restrict__ s2, double delta) {
     __shared__ double red[256];
-    spmv_rows<V>(
+    spmv_rows<V, 4>(
         M, [&](int c) { return ld_ro(x + c); },
         [&](int row, V s) {
             if (EPI == kEpiStore) {
