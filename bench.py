@@ -846,7 +846,7 @@ def main() -> None:
     e2e = {"value": round(ab64["step"] / e2e_s / 1e9, 2), "unit": "GB/s", "h2d_bytes_per_step": 8 * m,
            "d2h_bytes_per_step": 8 * m, "us_per_step": round(e2e_s * 1e6, 1),
            "note": "host wall time of each help_pcg_matvec call (synchronous): the input read from the host "
-                           "array by a copy kernel, both passes, the last one storing straight into the host "
+                           "array by a copy kernel, both passes, a copy kernel writing the host "
                            "output array (Grace: pageable host memory through the host page tables; "
                            "cudaMemcpyAsync copies where the device cannot)"}
 

@@ -196,8 +196,14 @@ int d2h(help_pcg* ctx, double* dst, const double* src, size_t n) {
 // for cudaMemcpyAsync from pageable memory, and no staging.  The kernel reads
 // the source after h2d_direct returns, so only calls that wait for their
 // stream before returning use it (the caller's arrays stay valid for the
-// duration of the call); those calls also let their last kernel store its
-// result straight into the caller's output array.
+// duration of the call); those calls also let their last pass store its
+// rows straight into the caller's output array where the rows come in index
+// order (A's own CSR / CSC: a warp's stores are contiguous), and write the
+// sliced layout's results (rows permuted within windows, so their stores
+// would cross the host link as scattered 8-byte writes) with one coalesced
+// copy kernel: (A D^-1 A^T) v on config 1 85.5 -> 74 us per call; the same
+// copy kernel after config 4's A v / A^T y (row order) cost 0.97 -> 1.09 /
+// 1.04 -> 1.34 ms, so those keep the direct stores.
 int h2d_direct(help_pcg* ctx, double* dst, const double* src, size_t n) {
     if (!ctx->host_direct) return h2d(ctx, dst, src, n);
     CK(vec_copy(src, dst, (int64_t)n, ctx->num_sms, ctx->stream));
@@ -1183,9 +1189,17 @@ static int help_pcg_matvec_body(help_pcg* ctx, int32_t op, const double* x, doub
     if (op < HELP_OP_A || op > HELP_OP_BT) return fail(ctx, HELP_E_ARG, "matvec: unknown op");
     if (op >= HELP_OP_ADAT && !ctx->renewed) return fail(ctx, HELP_E_ARG, "matvec: renew first");
     int rc = h2d_direct(ctx, ctx->xacc.as<double>(), x, nin);
-    // with direct host access the last pass stores its rows straight into y
-    if (!rc) rc = help_pcg_matvec_dev(ctx, op, 0, ctx->xacc.p, ctx->host_direct ? (void*)y : ctx->res.p,
-                                      (void*)ctx->stream);
+    // with direct host access the last pass stores into y itself where its
+    // rows come in index order (A, A^T); the sliced layout's (B, B^T and the
+    // second pass of A D^-1 A^T) stores into device memory, and one coalesced
+    // copy kernel writes y
+    const bool sliced = op != HELP_OP_A && op != HELP_OP_AT;
+    void* out = (ctx->host_direct && !sliced) ? (void*)y : ctx->res.p;
+    if (!rc) rc = help_pcg_matvec_dev(ctx, op, 0, ctx->xacc.p, out, (void*)ctx->stream);
+    if (!rc && ctx->host_direct && sliced) {
+        const cudaError_t e = vec_copy(ctx->res.as<double>(), y, (int64_t)nout, ctx->num_sms, ctx->stream);
+        if (e != cudaSuccess) rc = fail_cuda(ctx, e, "matvec");
+    }
     if (rc || ctx->host_direct) {
         // no kernel may still touch x or y after we return
         const cudaError_t e = cudaStreamSynchronize(ctx->stream);
@@ -1210,6 +1224,7 @@ static int help_pcg_matvec_acc_body(help_pcg* ctx, int32_t transpose, int32_t si
         const SpmvView<double> M = transpose ? view<double>(ctx->pl_csc, ctx->cp, ctx->ri, ctx->avT)
                                              : view<double>(ctx->pl_csr, ctx->rp, ctx->ci, ctx->av);
         // with direct host access the pass stores its rows straight into dest
+        // (rows in index order: a warp's stores are contiguous)
         double* out = ctx->host_direct ? dest : ctx->x2.as<double>();
         const cudaError_t e = spmv_launch<double>(kEpiAcc, M, ctx->xacc.as<double>(), out, ctx->res.as<double>(),
                                                   nullptr, nullptr, (double)sign, spmv_blocks(ctx), kSpmvThreads,
