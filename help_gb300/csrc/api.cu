@@ -174,7 +174,16 @@ SpmvView<V> view(const RowPlan& P, const DevMem& ptr, const DevMem& idx, const D
     return v;
 }
 
-int spmv_blocks(help_pcg* ctx) { return ctx->num_sms * 8; }
+// Standalone passes (grid-stride).  At scale, one wave of resident CTAs: a
+// grid past the resident count leaves a partial second wave (config 4's
+// product, 104M nonzeros: 3,094 -> 3,440 GB/s with one wave; the HSD
+// driver's A v 0.98 -> 0.87 ms).  Small passes keep 8 CTAs per SM, whose
+// extra blocks even out the few slices each block takes (config 1, 3.2M
+// nonzeros: 2,018 GB/s against 1,937 with one wave).
+constexpr int64_t kOneWaveNnz = 32 << 20;
+int spmv_blocks(help_pcg* ctx) {
+    return ctx->num_sms * (ctx->nnz >= kOneWaveNnz ? spmv_blocks_per_sm() : 8);
+}
 constexpr int kSpmvThreads = 256;
 
 // Host arrays of the caller straight to / from the copy engine.  A copy from
@@ -868,6 +877,9 @@ static int help_pcg_create_body(const help_pcg_options* opt, help_pcg** out) {
     if (e == cudaSuccess) e = cudaMallocHost((void**)&ctx->h_sc, sizeof(CgScalars));
     if (e != cudaSuccess) {
         release_all(ctx);
+        for (cudaEvent_t ev : {ctx->ev0, ctx->ev1})
+            if (ev) cudaEventDestroy(ev);
+        if (ctx->h_sc) cudaFreeHost(ctx->h_sc);
         if (ctx->stream) cudaStreamDestroy(ctx->stream);
         delete ctx;
         return e == cudaErrorMemoryAllocation ? HELP_E_NOMEM : HELP_E_CUDA;
@@ -955,11 +967,15 @@ static int help_pcg_construct_body(help_pcg* ctx, int32_t m, int32_t n, const in
     if (!rc) rc = alloc_vectors(ctx);
     if (rc) return rc;
     // CG kernels: grid-stride, grid sized to the work (small problems pay
-    // less for the per-block partial sums), at most 8 blocks per SM
+    // less for the per-block partial sums), at most one wave of resident
+    // CTAs of the graph kernels (6 per SM at their 40 registers; 8 per SM,
+    // a partial second wave, measured per FP64 iteration: config 3 100.1 ->
+    // 89.6 us, config 4 2,230 -> 2,047 us, config 2 365 -> 376 us)
     {
         const int64_t work = std::max<int64_t>(nnz, 32 * (int64_t)std::max(m, n));
         const int64_t nb = (work + 16383) / 16384;
-        ctx->cg_blocks = (int)std::max<int64_t>(8, std::min<int64_t>(nb, (int64_t)ctx->num_sms * 8));
+        ctx->cg_blocks =
+            (int)std::max<int64_t>(8, std::min<int64_t>(nb, (int64_t)ctx->num_sms * cg_blocks_per_sm()));
     }
     CK(ctx->cg_part.ensure(sizeof(double) * 4 * (size_t)ctx->cg_blocks));
     CK(cg_configure<double>(std::max(ctx->opt.pivots, 1)));

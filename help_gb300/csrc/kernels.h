@@ -78,6 +78,9 @@ cudaError_t cg_launch_init(const CgArgs<V>& A, int blocks, cudaStream_t st);
 template <class V>
 cudaError_t cg_launch_iteration(const CgArgs<V>& A, int blocks, cudaStream_t st);
 int cg_threads();
+// The fewest CTAs per SM any graph CG kernel (both precisions) keeps resident:
+// the CG grid is at most this many x SMs, one wave.
+int cg_blocks_per_sm();
 // Single-cluster CG (small systems): cluster size 16 / 8 / 0 = unavailable.
 template <class V>
 int cg_cluster_configure(int k_max);
@@ -136,6 +139,9 @@ cudaError_t vec_add_f32_scaled(double* x, const float* e, double scale, int64_t 
 cudaError_t vec_fill(double* x, double v, int64_t n, cudaStream_t st);
 // dst = src (either may be host memory the device reaches directly)
 cudaError_t vec_copy(const double* src, double* dst, int64_t n, int num_sms, cudaStream_t st);
+// The fewest CTAs per SM any standalone SpMV kernel keeps resident: the grid
+// of a standalone pass is this many x SMs, one wave.
+int spmv_blocks_per_sm();
 cudaError_t vec_fill_f32(float* x, float v, int64_t n, cudaStream_t st);
 // Deterministic sum of squares into out[0] (uses `part` of >= 1024 doubles).
 cudaError_t vec_sumsq(const double* x, int64_t n, double* part, double* out, cudaStream_t st);

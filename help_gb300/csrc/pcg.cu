@@ -28,6 +28,7 @@
 // dot products, alpha/beta and the pivot-block work stay in double.
 #include <cooperative_groups.h>
 
+#include <algorithm>
 #include <map>
 #include <mutex>
 
@@ -570,6 +571,34 @@ cudaError_t cg_launch_iteration(const CgArgs<V>& A, int blocks, cudaStream_t st)
 }
 
 int cg_threads() { return kCgThreads; }
+
+int cg_blocks_per_sm() {
+    static const int per_sm = [] {
+        int lo = 0;
+        auto take = [&](const void* f, size_t smem) {
+            int b = 0;
+            if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, f, kCgThreads, smem) == cudaSuccess && b > 0)
+                lo = lo ? std::min(lo, b) : b;
+        };
+        // dynamic shared memory: the k-vector copies are small against the
+        // register limit at the pivot counts of the graph path
+        take((const void*)k_p2<double>, 0);
+        take((const void*)k_p3<double>, 0);
+        take((const void*)k_p4<double>, 0);
+        take((const void*)k_a<double>, 0);
+        take((const void*)k_b<double>, 0);
+        take((const void*)k_c<double>, 0);
+        take((const void*)k_p2<float>, 0);
+        take((const void*)k_p3<float>, 0);
+        take((const void*)k_p4<float>, 0);
+        take((const void*)k_a<float>, 0);
+        take((const void*)k_b<float>, 0);
+        take((const void*)k_c<float>, 0);
+        cudaGetLastError();
+        return lo > 0 ? lo : 8;
+    }();
+    return per_sm;
+}
 
 // Cluster size for k_cg_cluster: 16 CTAs where the GPU can co-schedule such a
 // cluster with this shared memory, else 8 (the portable size); 0 if neither.

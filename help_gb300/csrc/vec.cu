@@ -112,6 +112,28 @@ inline int grid_for(int64_t n, int threads) {
 
 }  // namespace
 
+int spmv_blocks_per_sm() {
+    static const int per_sm = [] {
+        int lo = 0;
+        auto take = [&](const void* f) {
+            int b = 0;
+            if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, f, 256, 0) == cudaSuccess && b > 0)
+                lo = lo ? std::min(lo, b) : b;
+        };
+        take((const void*)k_spmv<double, kEpiStore>);
+        take((const void*)k_spmv<double, kEpiRhs>);
+        take((const void*)k_spmv<double, kEpiBacksub>);
+        take((const void*)k_spmv<double, kEpiResid>);
+        take((const void*)k_spmv<double, kEpiAddDelta>);
+        take((const void*)k_spmv<double, kEpiAcc>);
+        take((const void*)k_spmv<float, kEpiStore>);
+        take((const void*)k_spmv<float, kEpiAddDelta>);
+        cudaGetLastError();
+        return lo > 0 ? lo : 8;
+    }();
+    return per_sm;
+}
+
 template <class V, int E>
 cudaError_t spmv_launch_one(const SpmvView<V>& M, const V* x, V* y, const V* aux, const V* aux2, const double* s2,
                             double delta, int blocks, int threads, cudaStream_t stream) {

@@ -255,3 +255,26 @@ def test_direct_form_all_rows_pivots(name):
     ox1, ox2 = ora.SolveLinearEquation(d, b1, b2)
     assert rel(x2, ox2) < 1e-8
     assert rel(x1, ox1) < 1e-8
+
+
+@pytest.mark.parametrize("name", ["zipf", "longrows", "block"])
+def test_graph_cg_bitwise_repeatable(name):
+    """Two CG solves of the same system on the multi-kernel graph path give
+    bitwise the same solution and iteration count, in FP64 and FP32: every
+    reduction adds its blocks' partials in block order in the last block,
+    which takes its ticket only after every warp of every block has written
+    (k_p3's last block reads all of w = r_P - C^T z_N; these cases have C^T
+    rows taken by a warp each or split over CTAs)."""
+    lp = CASES[name]()
+    rng = np.random.default_rng(15)
+    d = np.exp(rng.uniform(-4, 4, lp.n))
+    b = rng.standard_normal(lp.m)
+    with backend.GpuNormalEquations(pivots=32, precision="mixed", cg_tol=1e-10, cg_max_iter=3000,
+                                    cg_path="graph") as g:
+        g.LinearEquation_Construct(lp)
+        g.RenewLinearEquation(d)
+        assert g.stats()["nnz_c"] > 0
+        for fp32 in (False, True):
+            (x1, i1), (x2, i2) = g.cg(b, fp32=fp32), g.cg(b, fp32=fp32)
+            assert g.stats()["cg_path_used"] == 1
+            assert i1 == i2 and np.array_equal(x1, x2), (name, fp32)
