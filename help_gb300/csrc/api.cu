@@ -53,8 +53,8 @@ double now_ms() {
 DevCtrl* ctrl_of(help_pcg* ctx) { return ctx->ctrl.as<DevCtrl>(); }
 
 int upload_split(help_pcg* ctx, RowSplit& S, const int32_t* ptr, int32_t rows, int g_min, int per_lane,
-                 const int32_t* idx, size_t elem) {
-    RowPlanHost h = plan_rows(ptr, rows, g_min, per_lane);
+                 const int32_t* idx, size_t elem, double order_waste) {
+    RowPlanHost h = plan_rows(ptr, rows, g_min, per_lane, order_waste);
     S.n_sell = 0;
     if (idx) {
         SellHost sh = plan_sell(ptr, idx, rows, h.short_max);
@@ -109,10 +109,11 @@ int upload_split(help_pcg* ctx, RowSplit& S, const int32_t* ptr, int32_t rows, i
 // idx (host column indices, may be null): also lay the short rows out in
 // slices for B's products (A and A^T, whose B values are refreshed at renew)
 int upload_plan(help_pcg* ctx, RowPlan& P, const int32_t* ptr, int32_t rows, bool with_f32,
-                const int32_t* idx = nullptr, int per_lane64 = kPerLaneF64, int per_lane32 = kPerLaneF32) {
+                const int32_t* idx = nullptr, int per_lane64 = kPerLaneF64, int per_lane32 = kPerLaneF32,
+                double order_waste = kOrderWaste) {
     P.rows = rows;
-    int rc = upload_split(ctx, P.s64, ptr, rows, kGminF64, per_lane64, idx, 8);
-    if (!rc && with_f32) rc = upload_split(ctx, P.s32, ptr, rows, kGminF32, per_lane32, idx, 4);
+    int rc = upload_split(ctx, P.s64, ptr, rows, kGminF64, per_lane64, idx, 8, order_waste);
+    if (!rc && with_f32) rc = upload_split(ctx, P.s32, ptr, rows, kGminF32, per_lane32, idx, 4, order_waste);
     return rc;
 }
 
@@ -773,7 +774,7 @@ int renew_impl(help_pcg* ctx, const double* d_host) {
     ctx->h_tmp.resize((size_t)m + 1);
     CK(cudaMemcpyAsync(ctx->h_tmp.data(), ctx->c_rp.p, 4 * ((size_t)m + 1), cudaMemcpyDeviceToHost, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
-    rc = upload_plan(ctx, ctx->pl_c, ctx->h_tmp.data(), m, mixed, nullptr, kPerLaneCF64, kPerLaneCF32);
+    rc = upload_plan(ctx, ctx->pl_c, ctx->h_tmp.data(), m, mixed, nullptr, kPerLaneCF64, kPerLaneCF32, kOrderWasteC);
     if (rc) return rc;
     std::vector<int32_t> ctp((size_t)k + 1, 0);
     if (k > 0) {

@@ -26,9 +26,15 @@ constexpr int32_t kLongRowMin = 4096;  // rows above this length are long
 constexpr int32_t kSegLen = 16384;     // nonzeros per segment of a long row (one CTA)
 constexpr int32_t kOrderWindow = 4096; // short rows are reordered only within windows of this many rows
 constexpr double kOrderWaste = 1.5;    // reorder when index order wastes this factor of lane steps
+// C = G[N, P] is rebuilt at every renew and its pass is bound by the FP64
+// pipe, which a warp's idle lanes still occupy: reorder at a smaller waste
+// (config 4's C: rows of ~85 entries, ~1.14 in index order)
+constexpr double kOrderWasteC = 1.05;
 
-// g_min: smallest group; per_lane: target nonzeros per lane of an average row.
-RowPlanHost plan_rows(const int32_t* ptr, int32_t rows, int32_t g_min, int32_t per_lane);
+// g_min: smallest group; per_lane: target nonzeros per lane of an average row;
+// short rows are reordered when index order wastes more than order_waste.
+RowPlanHost plan_rows(const int32_t* ptr, int32_t rows, int32_t g_min, int32_t per_lane,
+                      double order_waste = kOrderWaste);
 
 // Sliced layout of the short rows (length <= short_max) of one CSR matrix:
 // rows taken by decreasing length within windows of kOrderWindow rows, 32
