@@ -318,7 +318,7 @@ __global__ void __launch_bounds__(kTcThreads) k_mlp_fwd_tc(const __nv_bfloat16* 
         }
         if (ok) ok = mbar_wait(mbar, phase);
         phase ^= 1u;
-        ok = __syncthreads_and(ok);  // tcgen05.ld is warp-collective: one verdict for the CTA
+        ok = __syncthreads_and(ok);  // tcgen05.ld is warp-collective: one outcome for the whole CTA
         tc_fence_after();
         if (ok) tc_hidden_out(trow, s.b1, sh, tid);
         proxy_fence();
@@ -336,7 +336,7 @@ __global__ void __launch_bounds__(kTcThreads) k_mlp_fwd_tc(const __nv_bfloat16* 
         }
         if (ok) ok = mbar_wait(mbar, phase);
         phase ^= 1u;
-        ok = __syncthreads_and(ok);  // tcgen05.ld is warp-collective: one verdict for the CTA
+        ok = __syncthreads_and(ok);  // tcgen05.ld is warp-collective: one outcome for the whole CTA
         tc_fence_after();
         if (ok) tc_hidden_out(trow, s.b2, sh, tid);
         proxy_fence();
@@ -354,7 +354,7 @@ __global__ void __launch_bounds__(kTcThreads) k_mlp_fwd_tc(const __nv_bfloat16* 
         }
         if (ok) ok = mbar_wait(mbar, phase);
         phase ^= 1u;
-        ok = __syncthreads_and(ok);  // tcgen05.ld is warp-collective: one verdict for the CTA
+        ok = __syncthreads_and(ok);  // tcgen05.ld is warp-collective: one outcome for the whole CTA
         tc_fence_after();
         float v[16];
         if (ok) tc_ld16(trow, v);
