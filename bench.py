@@ -24,7 +24,7 @@ roofline of the dominant kernel and the SM clocks sampled during the timed
 region.
 
     python bench.py [--steps K] [--warmup W] [--gpus N] [--impl ours|reference] [--no-ipm] [--no-large]
-                    [--pcg-configs 0,1] [--pcg-iters I] [--pcg-only] [--mlp-only [--mlp-rows R]]
+                    [--pcg-configs 0,1] [--pcg-iters I] [--pcg-only] [--mlp-only [--mlp-rows R]] [--large-only]
 """
 from __future__ import annotations
 
@@ -720,6 +720,7 @@ def main() -> None:
     ap.add_argument("--no-ipm-large", action="store_true", help="skip the capped IPM runs on configs 1 and 4")
     ap.add_argument("--ipm-large-caps", default="1:25,4:45", help="config:seconds per arm of the capped IPM runs")
     ap.add_argument("--mlp-only", action="store_true", help="only the learned part's MLP rates (profiling runs)")
+    ap.add_argument("--large-only", action="store_true", help="only the 104M-nonzero product (profiling runs)")
     ap.add_argument("--mlp-rows", type=int, default=2_000_000, help="feature rows of the MLP rate measurement")
     args = ap.parse_args()
     if args.impl == "reference":
@@ -732,6 +733,13 @@ def main() -> None:
         torch.cuda.set_device(local)
         out = {c: pcg_rate(int(c), args.pcg_iters, local) for c in args.pcg_configs.split(",") if c}
         print(json.dumps({"pcg": out}), flush=True)
+        return
+    if args.large_only:
+        import torch
+
+        ws, rank, local = dist_env()
+        torch.cuda.set_device(local)
+        print(json.dumps({"spmv_large": spmv_large(max(1, args.steps), max(1, args.warmup), local)}), flush=True)
         return
     if args.mlp_only:
         import torch
