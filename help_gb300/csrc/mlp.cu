@@ -1,12 +1,14 @@
 // Learned part of the preconditioner: a 16 -> 64 -> 64 -> 2 MLP (ReLU) over
 // per-row features of the normal equations, in BF16 with FP32 accumulation
-// on the tensor cores (mma.sync m16n8k16), with its training kernels.
+// on the tensor cores: the inference forward on tcgen05 with TMEM
+// accumulators (k_mlp_fwd_tc, below), the training forward and backward on
+// mma.sync m16n8k16.
 //
 //   out[i, 0]  log-factor of a correction of the Schur diagonal D_S,i
 //   out[i, 1]  per-row scale of the warm start (previous solution of the
 //              same solve slot)
 //
-// Each warp takes tiles of 16 rows.  Forward: the accumulator fragment of
+// Training: each warp takes tiles of 16 rows.  Forward: the accumulator fragment of
 // one layer is exactly the A-operand fragment of the next (after ReLU and
 // rounding to BF16), so activations never leave registers; in training mode
 // they are also stored (BF16) for the backward pass.  Backward: per group of
@@ -319,6 +321,7 @@ __global__ void __launch_bounds__(kTcThreads) k_mlp_fwd_tc(const __nv_bfloat16* 
         if (ok) ok = mbar_wait(mbar, phase);
         phase ^= 1u;
         ok = __syncthreads_and(ok);  // tcgen05.ld is warp-collective: one outcome for the whole CTA
+        if (!ok) break;              // phase ^ 1 stays the pending phase for the wait below
         tc_fence_after();
         if (ok) tc_hidden_out(trow, s.b1, sh, tid);
         proxy_fence();
@@ -337,6 +340,7 @@ __global__ void __launch_bounds__(kTcThreads) k_mlp_fwd_tc(const __nv_bfloat16* 
         if (ok) ok = mbar_wait(mbar, phase);
         phase ^= 1u;
         ok = __syncthreads_and(ok);  // tcgen05.ld is warp-collective: one outcome for the whole CTA
+        if (!ok) break;              // phase ^ 1 stays the pending phase for the wait below
         tc_fence_after();
         if (ok) tc_hidden_out(trow, s.b2, sh, tid);
         proxy_fence();
@@ -355,6 +359,7 @@ __global__ void __launch_bounds__(kTcThreads) k_mlp_fwd_tc(const __nv_bfloat16* 
         if (ok) ok = mbar_wait(mbar, phase);
         phase ^= 1u;
         ok = __syncthreads_and(ok);  // tcgen05.ld is warp-collective: one outcome for the whole CTA
+        if (!ok) break;              // phase ^ 1 stays the pending phase for the wait below
         tc_fence_after();
         float v[16];
         if (ok) tc_ld16(trow, v);
@@ -369,7 +374,7 @@ __global__ void __launch_bounds__(kTcThreads) k_mlp_fwd_tc(const __nv_bfloat16* 
     }
     if (!ok) {
         // an MMA never signalled: give it one more bounded wait before the
-        // accumulator is freed, and mark the CTA's remaining rows
+        // accumulator is freed, and mark all of the CTA's rows
         if (tid == 0) mbar_wait(mbar, phase ^ 1u);
         for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
             const long long r = tile * kTcRows + tid;
