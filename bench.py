@@ -298,8 +298,31 @@ def ipm_time(config: int = 0) -> dict:
            L.generate(L.spec_mcf(24, 4, 3), 11))
     m_auto = ipm_run(0, "fp64", pivots=16, lp=mcf)
     m_graph = ipm_run(0, "fp64", pivots=16, lp=mcf, cg_path="graph")
-    plain["mcf"] = {"auto": m_auto, "graph": m_graph}
+    plain["mcf"] = {"auto": m_auto, "graph": m_graph, "paired": ipm_paired(mcf[1], 16, m_auto, mcf[0])}
+    plain["paired"] = ipm_paired(L.make_lp(config, 0), L.config_pivots(config), plain, "config %d" % config)
     return plain
+
+
+def ipm_paired(lp, k: int, single: dict, name: str) -> dict:
+    """The same plain FP64 IPM with the bottom system and the first search
+    direction of every iteration solved at once on two contexts (backend
+    solve2, help_pcg_pair); the run is bitwise the single context's."""
+    from help_gb300 import backend, hsd
+
+    with backend.GpuPairNormalEquations(pivots=min(k, lp.m), precision="fp64", cg_tol=1e-10, ir_tol=1e-10,
+                                        cg_max_iter=1_000_000) as p:
+        t0 = time.perf_counter()
+        r = hsd.solve_lp(lp, p.ne_backend())
+        wall = time.perf_counter() - t0
+        s0, s1 = p.stats(0), p.stats(1)
+    return {"workload": "%s: m=%d n=%d nnz=%d" % (name, lp.m, lp.n, lp.nnz),
+            "form": "plain FP64 PCG, k=%d, bottom system and first direction solved together on two contexts"
+                    % min(k, lp.m),
+            "seconds": round(wall, 3), "status": r["status"], "iterations": r["iterations"], "rel_gap": r["rel_gap"],
+            "primal_obj": r["primal_obj"], "solves": r["solves"],
+            "cg_iterations": int(s0["cg_iterations_total"] + s1["cg_iterations_total"]),
+            "same_objective_bitwise_as_single": bool(r["primal_obj"] == single["primal_obj"]),
+            "speedup_vs_single": round(single["seconds"] / wall, 3) if wall > 0 else None}
 
 
 def spmv_large(steps: int, warmup: int, local: int) -> dict:

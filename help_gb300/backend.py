@@ -42,32 +42,95 @@ def _f64(a, n=None) -> np.ndarray:
     return a
 
 
+def pcg_options(lib, pivots: int = 10, precision: str = "fp64", cg_tol: float = 1e-20,
+                cg_max_iter: int = 1_000_000, delta: float = 0.0, ir_tol: float = 1e-10,
+                ir_max_outer: int = 10, inner_tol: float = 1e-5, inner_max_iter: int = 200_000,
+                warm_start: bool = False, fallback: bool = True, device: int = 0, cg_path: str = "auto",
+                cap_ok: bool = False, mixed_max_d_spread: float = 1e8) -> native.PcgOptions:
+    """help_pcg_options from the library defaults and these arguments."""
+    o = native.PcgOptions()
+    lib.help_pcg_default_options(C.byref(o))
+    o.device = device
+    o.pivots = int(pivots)
+    o.precision = {"fp64": native.HELP_PREC_FP64, "mixed": native.HELP_PREC_MIXED}[precision]
+    o.cg_tol = cg_tol
+    o.cg_max_iter = int(cg_max_iter)
+    o.delta = delta
+    o.ir_tol = ir_tol
+    o.ir_max_outer = ir_max_outer
+    o.inner_tol = inner_tol
+    o.inner_max_iter = int(inner_max_iter)
+    o.warm_start = int(bool(warm_start))
+    o.fallback = int(bool(fallback))
+    o.cg_path = {"auto": 0, "graph": 1, "cluster": 2, "resident": 3}[cg_path]
+    o.cap_ok = int(bool(cap_ok))
+    o.mixed_max_d_spread = float(mixed_max_d_spread)
+    return o
+
+
+class GpuPairNormalEquations:
+    """Two contexts on one GB300 for the HSD driver's paired solves
+    (help_pcg_pair: the bottom system and the first search direction of
+    every IPM iteration solved at the same time, each on its own context,
+    host thread and stream).  Same options as GpuNormalEquations except the
+    warm start, which the pairing would reorder.  Use through ne_backend()."""
+
+    def __init__(self, **kw):
+        if kw.get("warm_start"):
+            raise ValueError("the pair runs every solve from a cold start")
+        self.lib = native.gpu_lib()
+        self.options = pcg_options(self.lib, **kw)
+        h = C.c_void_p()
+        rc = self.lib.help_pcg_pair_create(C.byref(self.options), C.byref(h))
+        if rc != 0:
+            raise BackendError(rc, "help_pcg_pair_create")
+        self.pair = h
+
+    def context(self, which: int):
+        return self.lib.help_pcg_pair_context(self.pair, which)
+
+    def stats(self, which: int = 0) -> dict:
+        s = native.PcgStats()
+        rc = self.lib.help_pcg_get_stats(self.context(which), C.byref(s))
+        if rc != 0:
+            raise BackendError(rc, "help_pcg_get_stats")
+        return {f: getattr(s, f) for f, _ in native.PcgStats._fields_}
+
+    def ne_backend(self) -> native.NeBackend:
+        """Backend table for help_hsd_solve with solve2 set."""
+        lib = self.lib
+        f = lambda fn: C.cast(fn, C.c_void_p).value
+        be = native.NeBackend(ctx=self.pair.value, construct=f(lib.help_pcg_pair_construct),
+                              renew=f(lib.help_pcg_pair_renew), solve=f(lib.help_pcg_pair_solve),
+                              destruct=f(lib.help_pcg_pair_destruct), matvec=f(lib.help_pcg_pair_matvec),
+                              solve2=f(lib.help_pcg_pair_solve2))
+        be._owner = self
+        return be
+
+    def close(self) -> None:
+        if getattr(self, "pair", None):
+            self.lib.help_pcg_pair_free(self.pair)
+            self.pair = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+
 class GpuNormalEquations:
     """Normal-equations backend on one GB300 (plain FP64 PCG or mixed precision)."""
 
-    def __init__(self, pivots: int = 10, precision: str = "fp64", cg_tol: float = 1e-20,
-                 cg_max_iter: int = 1_000_000, delta: float = 0.0, ir_tol: float = 1e-10,
-                 ir_max_outer: int = 10, inner_tol: float = 1e-5, inner_max_iter: int = 200_000,
-                 warm_start: bool = False, fallback: bool = True, device: int = 0, cg_path: str = "auto",
-                 cap_ok: bool = False, mixed_max_d_spread: float = 1e8):
+    def __init__(self, **kw):
         self.lib = native.gpu_lib()
-        o = native.PcgOptions()
-        self.lib.help_pcg_default_options(C.byref(o))
-        o.device = device
-        o.pivots = int(pivots)
-        o.precision = {"fp64": native.HELP_PREC_FP64, "mixed": native.HELP_PREC_MIXED}[precision]
-        o.cg_tol = cg_tol
-        o.cg_max_iter = int(cg_max_iter)
-        o.delta = delta
-        o.ir_tol = ir_tol
-        o.ir_max_outer = ir_max_outer
-        o.inner_tol = inner_tol
-        o.inner_max_iter = int(inner_max_iter)
-        o.warm_start = int(bool(warm_start))
-        o.fallback = int(bool(fallback))
-        o.cg_path = {"auto": 0, "graph": 1, "cluster": 2, "resident": 3}[cg_path]
-        o.cap_ok = int(bool(cap_ok))
-        o.mixed_max_d_spread = float(mixed_max_d_spread)
+        o = pcg_options(self.lib, **kw)
         self.options = o
         h = C.c_void_p()
         self._check(self.lib.help_pcg_create(C.byref(o), C.byref(h)), None)

@@ -28,7 +28,7 @@ GENCODE = "-gencode=arch=compute_103a,code=sm_103a"
 
 GPU_CU = ["api.cu", "pcg.cu", "pcg_resident.cu", "renew.cu", "dense.cu", "vec.cu", "adat.cu", "noalloc.cu", "mlp.cu",
           "learned.cu", "mlp_api.cu"]
-GPU_CPP = ["items.cpp"]
+GPU_CPP = ["items.cpp", "pair.cpp"]
 GPU_HDR = ["common.cuh", "spmv.cuh", "kernels.h", "context.h", "items.h", "mlp.h", "guard.h"]
 LP_CPP = ["lp_gen.cpp", "hsd.cpp", "lp_io.cpp", "lindep.cpp"]
 

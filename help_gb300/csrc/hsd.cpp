@@ -74,6 +74,7 @@ struct Hsd {
     std::vector<double> hat_r_xz, dx, dy, dz, dx_b, dy_b, dz_b;
     double hat_r_tk = 0, dtau = 0, dkappa = 0;
     std::vector<double> Dir_p, Dir_q, Dir_u, Dir_v, Dir_RHS1, Dir_RHS2, SLE_RHS1, SLE_RHS2, LEBOT_RHS1, LEBOT_RHS2;
+    std::vector<double> SLE2_RHS1, SLE2_RHS2;  // the second system of a paired solve (backend solve2)
     std::vector<double> masked;  // hrxz where x < z, for the device product
     double backend_s = 0;
     int solves = 0, renews = 0;
@@ -122,6 +123,13 @@ struct Hsd {
         if (be->solve(be->ctx, D.data(), b1, b2, x1, x2) != 0) be_error = 1;
         backend_s += now_s() - t;
         solves++;
+    }
+    void Solve2(const double* b1a, const double* b2a, double* x1a, double* x2a, const double* b1b, const double* b2b,
+                double* x1b, double* x2b) {
+        const double t = now_s();
+        if (be->solve2(be->ctx, D.data(), b1a, b2a, x1a, x2a, b1b, b2b, x1b, x2b) != 0) be_error = 1;
+        backend_s += now_s() - t;
+        solves += 2;
     }
 
     // HSDSolver.cpp:53-150
@@ -173,6 +181,17 @@ struct Hsd {
         Solve(SLE_RHS1.data(), SLE_RHS2.data(), p, q);
         for (int i = 0; i < m; i++) q[i] = -q[i];
     }
+    // Two SolveLE at once (backend solve2): each system as SolveLE does it
+    void SolveLE2(const double* sa, const double* ta, double* pa, double* qa, const double* sb, const double* tb,
+                  double* pb, double* qb) {
+        for (int i = 0; i < n; i++) SLE_RHS1[i] = sa[i];
+        for (int i = 0; i < m; i++) SLE_RHS2[i] = ta[i];
+        for (int i = 0; i < n; i++) SLE2_RHS1[i] = sb[i];
+        for (int i = 0; i < m; i++) SLE2_RHS2[i] = tb[i];
+        Solve2(SLE_RHS1.data(), SLE_RHS2.data(), pa, qa, SLE2_RHS1.data(), SLE2_RHS2.data(), pb, qb);
+        for (int i = 0; i < m; i++) qa[i] = -qa[i];
+        for (int i = 0; i < m; i++) qb[i] = -qb[i];
+    }
 
     // HSDSolver.cpp:212-220
     double MixDots(const double* p, const double* q) const {
@@ -189,11 +208,37 @@ struct Hsd {
         return MixDots(Dir_p.data(), Dir_q.data());
     }
 
-    // HSDSolver.cpp:281-473
+    // HSDSolver.cpp:281-473, in three parts so that a backend with solve2 can
+    // take the direction's system together with the bottom one: the
+    // right-hand side (DirRhs, returns UP), the solve, the rest (DirFinish).
     int SearchDirection(double eta, double DOT, double* hrxz, double hrtk, double* ddx, double& ddtau, double* ddy,
                         double* ddz, double& ddkappa) {
+        const double UP = DirRhs(eta, hrxz, hrtk);
+        SolveLE(Dir_RHS1.data(), Dir_RHS2.data(), Dir_u.data(), Dir_v.data());
+        return DirFinish(eta, DOT, hrxz, hrtk, UP, ddx, ddtau, ddy, ddz, ddkappa);
+    }
+
+    // LinearEquationBottom and the first SearchDirection of an iteration.
+    // Neither right-hand side depends on the other system's solution, so with
+    // the backend's solve2 both systems are solved at once; every value the
+    // driver computes is the same as in the sequential order.
+    int BottomAndDirection(double eta, double* hrxz, double hrtk, double* ddx, double& ddtau, double* ddy,
+                           double* ddz, double& ddkappa, double& DOT) {
+        if (!be->solve2) {
+            DOT = LinearEquationBottom();
+            return SearchDirection(eta, DOT, hrxz, hrtk, ddx, ddtau, ddy, ddz, ddkappa);
+        }
+        for (int i = 0; i < n; i++) LEBOT_RHS1[i] = lp->c[i];
+        for (int i = 0; i < m; i++) LEBOT_RHS2[i] = -lp->b[i];
+        const double UP = DirRhs(eta, hrxz, hrtk);
+        SolveLE2(LEBOT_RHS1.data(), LEBOT_RHS2.data(), Dir_p.data(), Dir_q.data(), Dir_RHS1.data(), Dir_RHS2.data(),
+                 Dir_u.data(), Dir_v.data());
+        DOT = MixDots(Dir_p.data(), Dir_q.data());
+        return DirFinish(eta, DOT, hrxz, hrtk, UP, ddx, ddtau, ddy, ddz, ddkappa);
+    }
+
+    double DirRhs(double eta, double* hrxz, double hrtk) {
         const double* c = lp->c;
-        const double* b = lp->b;
         SetScaledVector(n, eta, r_d.data(), Dir_RHS1.data());
         SetScaledVector(m, eta, r_p.data(), Dir_RHS2.data());
         for (int i = 0; i < n; i++) hrxz[i] /= std::max(x[i], z[i]);
@@ -216,8 +261,14 @@ struct Hsd {
         double UP = eta * r_g + hrtk / tau;
         for (int i = 0; i < n; i++)
             if (x[i] < z[i]) UP += c[i] * hrxz[i];
+        return UP;
+    }
+
+    int DirFinish(double eta, double DOT, const double* hrxz, double hrtk, double UP, double* ddx, double& ddtau,
+                  double* ddy, double* ddz, double& ddkappa) {
+        const double* c = lp->c;
+        const double* b = lp->b;
         const double DOWN = D_g - DOT;
-        SolveLE(Dir_RHS1.data(), Dir_RHS2.data(), Dir_u.data(), Dir_v.data());
         if (DOWN <= 1e-13)
             ddtau = 0;
         else
@@ -335,13 +386,13 @@ struct Hsd {
         CalcNewtonParameters();
         if (status != HSD_STATUS_OK) return;
         Renew();
-        const double DOT = LinearEquationBottom();
         double phi = 1.0;
         const double eta = 1.0;
         for (int i = 0; i < n; i++) hat_r_xz[i] = -x[i] * z[i] + mu_;
         hat_r_tk = -tau * kappa + mu_;
-        const int Newton_Success =
-            SearchDirection(eta, DOT, hat_r_xz.data(), hat_r_tk, dx.data(), dtau, dy.data(), dz.data(), dkappa);
+        double DOT = 0.0;
+        const int Newton_Success = BottomAndDirection(eta, hat_r_xz.data(), hat_r_tk, dx.data(), dtau, dy.data(),
+                                                      dz.data(), dkappa, DOT);
         double p_step = 0, d_step = 0;
         if (Newton_Success)
             GetStepsize(p_step, d_step);
@@ -414,13 +465,13 @@ struct Hsd {
                 break;
             }
             Renew();
-            const double DOT = LinearEquationBottom();
             const double phi = 1.0;
             double eta = 1.0;
             for (int i = 0; i < n; i++) hat_r_xz[i] = -x[i] * z[i];
             hat_r_tk = -tau * kappa;
-            const int Newton_Success =
-                SearchDirection(eta, DOT, hat_r_xz.data(), hat_r_tk, dx.data(), dtau, dy.data(), dz.data(), dkappa);
+            double DOT = 0.0;
+            const int Newton_Success = BottomAndDirection(eta, hat_r_xz.data(), hat_r_tk, dx.data(), dtau, dy.data(),
+                                                          dz.data(), dkappa, DOT);
             double p_step = 0.0, d_step = 0.0, gamma;
             if (Newton_Success) {
                 GetStepsize(p_step, d_step);
@@ -497,6 +548,10 @@ static int hsd_solve(const help_lp* lp, const help_ne_backend* be, const help_hs
                     &h.Dir_RHS1, &h.SLE_RHS1, &h.LEBOT_RHS1})
         v->assign(n, 0.0);
     if (be->matvec) h.masked.assign(n, 0.0);
+    if (be->solve2) {
+        h.SLE2_RHS1.assign(n, 0.0);
+        h.SLE2_RHS2.assign(m, 0.0);
+    }
     for (auto* v : {&h.y, &h.r_p, &h.dy, &h.dy_b, &h.Dir_q, &h.Dir_v, &h.Dir_RHS2, &h.SLE_RHS2, &h.LEBOT_RHS2})
         v->assign(m, 0.0);
     double tb = now_s();

@@ -143,6 +143,7 @@ class NeBackend(C.Structure):
         ("solve", C.c_void_p),
         ("destruct", C.c_void_p),
         ("matvec", C.c_void_p),  # optional: dest += sign * A v / A^T v (NULL: the driver's host loops)
+        ("solve2", C.c_void_p),  # optional: two solves at once (NULL: one after the other)
     ]
 
 
@@ -190,6 +191,9 @@ GPU_SYMBOLS = [
     "help_pcg_get_pivots", "help_pcg_cg", "help_pcg_cg_f32", "help_adat_assemble", "help_adat_matvec_noalloc",
     "help_mlp_create", "help_mlp_free", "help_mlp_last_error", "help_mlp_set_params", "help_mlp_get_params",
     "help_mlp_forward", "help_mlp_loss_grad", "help_mlp_train_step", "help_pcg_attach_mlp", "help_pcg_features",
+    "help_pcg_pair_create", "help_pcg_pair_free", "help_pcg_pair_context", "help_pcg_pair_construct",
+    "help_pcg_pair_renew", "help_pcg_pair_solve", "help_pcg_pair_solve2", "help_pcg_pair_destruct",
+    "help_pcg_pair_matvec",
 ]
 LP_SYMBOLS = [
     "help_lp_generate", "help_lp_free", "help_lp_write_mps", "help_csc_to_csr", "help_lp_read_mps",
@@ -236,6 +240,11 @@ def gpu_lib() -> C.CDLL:
         lib.help_pcg_cg_f32.argtypes = [vp, dp, dp, C.POINTER(C.c_int64)]
         lib.help_adat_assemble.argtypes = [vp, dp, dp, dp, dp, C.POINTER(C.c_int64)]
         lib.help_adat_matvec_noalloc.argtypes = [i32, i32, i64] + [vp] * 10
+        lib.help_pcg_pair_create.argtypes = [C.POINTER(PcgOptions), C.POINTER(C.c_void_p)]
+        lib.help_pcg_pair_free.argtypes = [vp]
+        lib.help_pcg_pair_free.restype = None
+        lib.help_pcg_pair_context.argtypes = [vp, i32]
+        lib.help_pcg_pair_context.restype = vp
         lib.help_mlp_create.argtypes = [i32, C.POINTER(C.c_void_p)]
         lib.help_mlp_free.argtypes = [vp]
         lib.help_mlp_last_error.argtypes = [vp]

@@ -165,6 +165,35 @@ int help_pcg_matvec_dev(help_pcg* ctx, int32_t op, int32_t fp32, const void* x, 
  * optional matvec of its backend table.  Each row's products are summed on
  * the device and added to dest once. */
 int help_pcg_matvec_acc(help_pcg* ctx, int32_t transpose, int32_t sign, const double* v, double* dest);
+
+/* Two contexts on one GPU for the HSD driver's paired solves (help_lp.h,
+ * help_ne_backend.solve2).  Each IPM iteration solves the bottom system
+ * (LinearEquationBottom, HSDSolver.cpp:226-261) and the first search
+ * direction (:281-473) with the same matrix, and neither right-hand side
+ * depends on the other's solution: the pair gives each to its own context,
+ * on its own host thread and stream, so the two CG runs overlap on the GPU
+ * (two single-cluster runs on small systems).  Both contexts are built and
+ * renewed from the same arguments; each solve gives what help_pcg_solve on
+ * one context gives (a cold start each: no warm start, no learned part).
+ * The backend-table entries take the pair as their ctx. */
+typedef struct help_pcg_pair help_pcg_pair;
+int help_pcg_pair_create(const help_pcg_options* opt, help_pcg_pair** out);
+void help_pcg_pair_free(help_pcg_pair* pair);
+/* Context 0 or 1 of the pair (stats, products); NULL for any other index. */
+help_pcg* help_pcg_pair_context(help_pcg_pair* pair, int32_t which);
+int help_pcg_pair_construct(void* pair, int32_t m, int32_t n, const int32_t* col_ptr, const int32_t* row_ind,
+                            const double* val);
+int help_pcg_pair_renew(void* pair, const double* d);
+/* One solve, on context 0. */
+int help_pcg_pair_solve(void* pair, const double* d, const double* b_1, const double* b_2, double* x_1,
+                        double* x_2);
+/* (b_1a, b_2a) on context 0 and (b_1b, b_2b) on context 1, at the same time;
+ * the first error code of the two (context 0's first). */
+int help_pcg_pair_solve2(void* pair, const double* d, const double* b_1a, const double* b_2a, double* x_1a,
+                         double* x_2a, const double* b_1b, const double* b_2b, double* x_1b, double* x_2b);
+int help_pcg_pair_destruct(void* pair);
+/* help_pcg_matvec_acc on context 0. */
+int help_pcg_pair_matvec(void* pair, int32_t transpose, int32_t sign, const double* v, double* dest);
 /* z = M^-1 r with the last renew's partial-Cholesky preconditioner
  * (Preconditioner, PCG.cpp:183-196), vectors in the original row order. */
 int help_pcg_precond_apply(help_pcg* ctx, const double* r, double* z);

@@ -140,6 +140,15 @@ typedef struct help_ne_backend {
      * driver's own products (ATimes, Helper.cpp:110-152) done where A
      * already lives.  NULL: the driver's host loops (the reference's order). */
     int (*matvec)(void* ctx, int32_t transpose, int32_t sign, const double* v, double* dest);
+    /* Optional (may be NULL): two solves with the matrix of the last renew,
+     * (b_1a, b_2a) -> (x_1a, x_2a) and (b_1b, b_2b) -> (x_1b, x_2b), each giving
+     * what solve gives for it, run at the same time where the backend can.
+     * The driver then solves the bottom system (LinearEquationBottom,
+     * HSDSolver.cpp:226-261) and the first direction of an iteration
+     * (SearchDirection, :281-473) together: neither right-hand side depends on
+     * the other's solution.  NULL: one solve after the other, as the reference. */
+    int (*solve2)(void* ctx, const double* d, const double* b_1a, const double* b_2a, double* x_1a,
+                  double* x_2a, const double* b_1b, const double* b_2b, double* x_1b, double* x_2b);
 } help_ne_backend;
 
 typedef struct help_hsd_options {

@@ -95,3 +95,31 @@ def test_ungrounded_flow_presolved_then_solved():
     for j in range(full.n):
         A[full.row_ind[full.col_ptr[j]:full.col_ptr[j + 1]], j] = full.val[full.col_ptr[j]:full.col_ptr[j + 1]]
     assert np.linalg.norm(A @ runs[0]["x"] - full.b) <= 1e-7 * (1 + np.linalg.norm(full.b))
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("name, spec, seed", [("random", L.spec_random(400, 1200, 5), 21),
+                                              ("mcf", L.spec_mcf(10, 3, 3), 22)])
+def test_paired_solves_give_the_same_run(precision, name, spec, seed):
+    """The bottom system and the first direction of every iteration solved
+    at once on two contexts (backend solve2, help_pcg_pair) give bitwise the
+    run of one context solving them one after the other: each solve is a cold
+    start, and the driver computes the same values in the same order."""
+    lp = L.generate(spec, seed)
+    kw = dict(pivots=10, precision=precision, cg_tol=1e-10, ir_tol=1e-10, cg_max_iter=200_000)
+    with backend.GpuNormalEquations(**kw) as g:
+        one = hsd.solve_lp(lp, g.ne_backend(), want_solution=True)
+    with backend.GpuPairNormalEquations(**kw) as p:
+        two = hsd.solve_lp(lp, p.ne_backend(), want_solution=True)
+        s0, s1 = p.stats(0), p.stats(1)
+    assert one["status"] == two["status"] == 0 and one["iterations"] == two["iterations"], (name, one, two)
+    assert one["solves"] == two["solves"]
+    assert one["primal_obj"] == two["primal_obj"] and one["rel_gap"] == two["rel_gap"]
+    assert np.array_equal(one["x"], two["x"]) and np.array_equal(one["y"], two["y"])
+    # context 1 took the second system of every pair: one per direction computed
+    assert s1["solves"] > 0 and s0["solves"] + s1["solves"] == one["solves"]
+
+
+def test_pair_rejects_warm_start():
+    with pytest.raises(ValueError):
+        backend.GpuPairNormalEquations(pivots=4, warm_start=True)
