@@ -132,6 +132,7 @@ RENEW_FN = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_void_p)
 SOLVE_FN = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p)
 DESTRUCT_FN = C.CFUNCTYPE(C.c_int, C.c_void_p)
 MATVEC_FN = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p)
+SOLVE2_FN = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_void_p, *([C.c_void_p] * 8))
 ONITER_FN = C.CFUNCTYPE(None, C.c_void_p, C.c_int32, C.POINTER(C.c_double))
 
 

@@ -195,3 +195,34 @@ def test_hsd_driver_wall_clock_cap():
     ora2 = ob.OracleNormalEquations(pivots=10, tol=1e-10)
     capped = hsd.solve_lp(lp, ora2.ne_backend(), max_seconds=1e-9)
     assert capped["status"] == 2 and capped["iterations"] == 1 and capped["renews"] <= 1
+
+
+def test_hsd_driver_paired_solves_give_the_same_run():
+    """With a backend that offers solve2, the driver computes the bottom
+    system's and the first direction's right-hand sides and solves them in
+    one call; every value it computes is the same as in the reference's
+    order.  Here solve2 is the CPU oracle's solve done twice, so the run must
+    equal the sequential one bit for bit."""
+    import ctypes as C
+    from help_gb300 import native
+    lp = L.generate(L.spec_random(80, 240, 5), 3)
+    seq = ob.OracleNormalEquations(pivots=10, tol=1e-14, max_iter=10**6)
+    r1 = hsd.solve_lp(lp, seq.ne_backend(), want_solution=True)
+    ora = ob.OracleNormalEquations(pivots=10, tol=1e-14, max_iter=10**6)
+    base = ora.ne_backend()
+    solve = native.SOLVE_FN(base.solve)
+    pairs = []
+
+    def solve2(ctx, d, b1a, b2a, x1a, x2a, b1b, b2b, x1b, x2b):
+        pairs.append(1)
+        rc = solve(ctx, d, b1a, b2a, x1a, x2a)
+        return rc if rc else solve(ctx, d, b1b, b2b, x1b, x2b)
+
+    fn = native.SOLVE2_FN(solve2)
+    be = native.NeBackend(ctx=base.ctx, construct=base.construct, renew=base.renew, solve=base.solve,
+                          destruct=base.destruct, solve2=C.cast(fn, C.c_void_p).value)
+    r2 = hsd.solve_lp(lp, be, want_solution=True)
+    assert r1["status"] == r2["status"] == 0 and r1["iterations"] == r2["iterations"]
+    assert r1["solves"] == r2["solves"] and len(pairs) == r1["iterations"]
+    assert r1["primal_obj"] == r2["primal_obj"] and r1["rel_gap"] == r2["rel_gap"]
+    assert np.array_equal(r1["x"], r2["x"]) and np.array_equal(r1["y"], r2["y"])
