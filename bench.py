@@ -546,30 +546,20 @@ def ipm_large(params, local: int, caps: dict) -> dict:
             except Exception as e:
                 res[arm] = {"error": str(e)}
         if config == 1:
-            # plain FP64 again with the bottom system and first direction of
+            # both arms again with the bottom system and first direction of
             # each iteration solved together on two contexts (help_pcg_pair)
-            try:
-                res["plain_fp64_paired"] = ipm_capped_paired(lp, k, cap, local)
-            except Exception as e:
-                res["plain_fp64_paired"] = {"error": str(e)}
+            for arm, prm, prec in (("plain_fp64_paired", None, "fp64"), ("learned_mixed_paired", params, "mixed")):
+                try:
+                    r = learned.evaluate(lp, k, prm, cg_tol=1e-10, device=local, precision=prec, max_seconds=cap,
+                                         cg_max_iter=20000, cap_ok=True, trace=True, paired=True)
+                    r["seconds"] = round(r["seconds"], 2)
+                    r["time_to_1e-8_s"] = r["seconds"] if r["status"] == 0 and r["rel_gap"] <= 1e-8 else None
+                    res[arm] = r
+                except Exception as e:
+                    res[arm] = {"error": str(e)}
         out["config%d" % config] = res
         del lp
     return out
-
-
-def ipm_capped_paired(lp, k: int, cap: float, local: int) -> dict:
-    from help_gb300 import backend, hsd
-
-    with backend.GpuPairNormalEquations(pivots=k, precision="fp64", cg_tol=1e-10, ir_tol=1e-10, cg_max_iter=20000,
-                                        cap_ok=True, device=local) as p:
-        t0 = time.perf_counter()
-        r = hsd.solve_lp(lp, p.ne_backend(), max_seconds=cap)
-        wall = time.perf_counter() - t0
-        cg = int(p.stats(0)["cg_iterations_total"] + p.stats(1)["cg_iterations_total"])
-    return {"status": r["status"], "iterations": r["iterations"], "primal_obj": r["primal_obj"],
-            "rel_gap": r["rel_gap"], "primal_infeas": r["primal_infeas"], "dual_infeas": r["dual_infeas"],
-            "cg_iterations": cg, "seconds": round(wall, 2),
-            "time_to_1e-8_s": round(wall, 2) if r["status"] == 0 and r["rel_gap"] <= 1e-8 else None}
 
 
 def learned_ablation() -> dict:

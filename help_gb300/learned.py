@@ -27,7 +27,7 @@ import time
 import numpy as np
 
 from . import native
-from .backend import GpuNormalEquations
+from .backend import GpuNormalEquations, GpuPairNormalEquations
 
 
 FEATURES = 11   # features in use per row (include/help_gpu.h); the rest of the 16 are zero
@@ -412,40 +412,59 @@ def train(data: dict, steps: int = 600, lr: float = 3e-3, seed: int = 0, device:
 
 def evaluate(lp, pivots: int, params: np.ndarray | None, cg_tol: float = 1e-10, device: int = 0,
              precision: str = "fp64", max_seconds: float = 0.0, cg_max_iter: int = 200_000,
-             cap_ok: bool = False, trace: bool = False) -> dict:
+             cap_ok: bool = False, trace: bool = False, paired: bool = False) -> dict:
     """One IPM run; with ``params`` the model is attached; precision "mixed"
     runs the FP32-in-FP64-refinement form (refined to cg_tol).
     ``max_seconds`` caps the run's wall time; ``cap_ok`` lets a solve that
     stops at ``cg_max_iter`` hand back its inexact direction; ``trace``
     records (seconds, rel gap, primal / dual infeasibility, CG iterations so
-    far) at every iteration."""
+    far) at every iteration.  ``paired``: the bottom system and the first
+    direction of every iteration solved together on two contexts
+    (GpuPairNormalEquations), the model attached to both.  Each context's
+    solve slots keep one role -- context 0 the bottom system then the
+    corrector, context 1 the predictor -- so every warm start comes from the
+    previous renew's solution of the same system, as on one context; the
+    Schur-diagonal correction, which a context computes at renew from its
+    first slot's features, follows the predictor's history on context 1
+    (the bottom system's on one context), so the run is close to, not
+    bitwise, the single context's."""
     from . import hsd
 
     mlp = Mlp(device, params) if params is not None else None
     rows = []
-    with GpuNormalEquations(pivots=pivots, cg_tol=cg_tol, cg_max_iter=cg_max_iter, device=device,
-                            precision=precision, ir_tol=cg_tol, cap_ok=cap_ok) as ne:
+    kw = dict(pivots=pivots, cg_tol=cg_tol, cg_max_iter=cg_max_iter, device=device, precision=precision,
+              ir_tol=cg_tol, cap_ok=cap_ok)
+    with (GpuPairNormalEquations(**kw) if paired else GpuNormalEquations(**kw)) as ne:
+        lib = ne.lib
+        ctxs = [ne.context(0), ne.context(1)] if paired else [ne.ctx]
+        stats = (lambda: [ne.stats(0), ne.stats(1)]) if paired else (lambda: [ne.stats()])
+        total = lambda key: int(sum(s_[key] for s_ in stats()))
+
+        def attach(h):
+            for c in ctxs:
+                rc = lib.help_pcg_attach_mlp(c, h)
+                if rc != native.HELP_OK:
+                    raise RuntimeError("help_pcg_attach_mlp failed (%d)" % rc)
+
         if mlp is not None:
-            ne._check(ne.lib.help_pcg_attach_mlp(ne.ctx, mlp.h))
+            attach(mlp.h)
         t0 = time.perf_counter()
 
         def on_iter(it, s):
-            rows.append([round(time.perf_counter() - t0, 3), s[2], s[3], s[4],
-                         int(ne.stats()["cg_iterations_total"])])
+            rows.append([round(time.perf_counter() - t0, 3), s[2], s[3], s[4], total("cg_iterations_total")])
 
         r = hsd.solve_lp(lp, ne.ne_backend(), max_seconds=max_seconds, on_iter=on_iter if trace else None)
         wall = time.perf_counter() - t0
-        st = ne.stats()
+        cg_total, fallbacks = total("cg_iterations_total"), total("learned_fallbacks")
         if mlp is not None:
-            ne._check(ne.lib.help_pcg_attach_mlp(ne.ctx, None))
+            attach(None)
     if mlp is not None:
         mlp.close()
     if r["rc"] != 0:
         raise RuntimeError("IPM backend error (rc %d)" % r["rc"])
     out = {"status": r["status"], "iterations": r["iterations"], "primal_obj": r["primal_obj"],
            "rel_gap": r["rel_gap"], "primal_infeas": r["primal_infeas"], "dual_infeas": r["dual_infeas"],
-           "cg_iterations": int(st["cg_iterations_total"]), "seconds": wall,
-           "learned_fallbacks": int(st["learned_fallbacks"])}
+           "cg_iterations": cg_total, "seconds": wall, "learned_fallbacks": fallbacks}
     if trace:
         out["trace"] = {"columns": ["s", "rel_gap", "primal_infeas", "dual_infeas", "cg_iterations"], "rows": rows}
     return out

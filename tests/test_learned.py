@@ -104,3 +104,23 @@ def test_ipm_learned_mixed_matches_plain(trained):
         assert plain["status"] == 0 and lm["status"] == 0
         assert abs(plain["primal_obj"] - lm["primal_obj"]) / abs(plain["primal_obj"]) < 1e-6
         assert lm["rel_gap"] < 1e-8
+
+
+def test_ipm_learned_paired_reaches_the_same_optimum(trained):
+    """The learned part with the bottom system and first direction of every
+    iteration solved together on two contexts (the model attached to both).
+    Each context's solve slots keep one role, so every warm start comes from
+    the same system as on one context; the Schur-diagonal correction, which a
+    context computes at renew from its first slot's features, follows the
+    predictor's history on context 1 instead of the bottom system's, so CG
+    iteration counts differ slightly.  The run reaches the same optimum."""
+    from help_gb300 import learned
+
+    params, _ = trained
+    lp = L.generate(L.spec_mcf(**SPEC), TEST_SEEDS[0])
+    for prec in ("fp64", "mixed"):
+        one = learned.evaluate(lp, PIVOTS, params, precision=prec)
+        two = learned.evaluate(lp, PIVOTS, params, precision=prec, paired=True)
+        assert one["status"] == two["status"] == 0
+        assert abs(one["primal_obj"] - two["primal_obj"]) <= 1e-9 * abs(one["primal_obj"]), (prec, one, two)
+        assert abs(one["cg_iterations"] - two["cg_iterations"]) <= 0.05 * one["cg_iterations"], (prec, one, two)
