@@ -1062,7 +1062,8 @@ static int help_pcg_solve_body(help_pcg* ctx, const double* d, const double* b_1
                            ctx->rhs.as<double>(), ctx->b2.as<double>(), nullptr, nullptr, 0.0, spmv_blocks(ctx),
                            kSpmvThreads, ctx->stream));
     // x_2 (UsePCG_CPU.cpp:154-166)
-    const int slot = std::min(ctx->solve_slot, kSolveSlots - 1);
+    const int slot = ctx->solve_slot < ctx->slot_map_n ? ctx->slot_map[ctx->solve_slot]
+                                                       : std::min(ctx->solve_slot, kSolveSlots - 1);
     bool warm = ctx->opt.warm_start && ctx->have_prev_x2;
     bool learned_warm = false;
     if (ctx->mlp_active) {
@@ -1371,6 +1372,38 @@ static int help_pcg_attach_mlp_body(help_pcg* ctx, help_mlp* mlp) {
 
 int help_pcg_attach_mlp(help_pcg* ctx, help_mlp* mlp) {
     return c_guard(HELP_E_NOMEM, [&] { return help_pcg_attach_mlp_body(ctx, mlp); });
+}
+
+int help_pcg_set_solve_slots(help_pcg* ctx, const int32_t* slots, int32_t n) {
+    if (!ctx || n < 0 || n > kSolveSlots || (n > 0 && !slots)) return HELP_E_ARG;
+    for (int32_t i = 0; i < n; ++i)
+        if (slots[i] < 0 || slots[i] >= kSolveSlots) return HELP_E_ARG;
+    for (int32_t i = 0; i < n; ++i) ctx->slot_map[i] = slots[i];
+    ctx->slot_map_n = n;
+    return HELP_OK;
+}
+
+static int help_pcg_share_solution_body(help_pcg* dst, int32_t dst_slot, help_pcg* src, int32_t src_slot) {
+    if (!dst || !src || dst_slot < 0 || dst_slot >= kSolveSlots || src_slot < 0 || src_slot >= kSolveSlots)
+        return HELP_E_ARG;
+    if (!dst->constructed || !src->constructed || dst->m != src->m || dst->device != src->device)
+        return fail(dst, HELP_E_ARG, "share_solution: both contexts constructed with the same matrix, same device");
+    help_pcg* ctx = dst;  // CK reports on the destination
+    const bool have = src->mlp && src->x2_have[src->x2_cur][src_slot];
+    dst->x2_have[dst->x2_cur][dst_slot] = false;
+    if (!have || !dst->mlp) return HELP_OK;
+    CK(cudaSetDevice(dst->device));
+    CK(cudaStreamSynchronize(src->stream));  // src's copy of that solution is complete
+    CK(dst->x2h[dst->x2_cur][dst_slot].ensure(8 * (size_t)dst->m));
+    CK(cudaMemcpyAsync(dst->x2h[dst->x2_cur][dst_slot].p, src->x2h[src->x2_cur][src_slot].p, 8 * (size_t)dst->m,
+                       cudaMemcpyDeviceToDevice, dst->stream));
+    CK(cudaStreamSynchronize(dst->stream));
+    dst->x2_have[dst->x2_cur][dst_slot] = true;
+    return HELP_OK;
+}
+
+int help_pcg_share_solution(help_pcg* dst, int32_t dst_slot, help_pcg* src, int32_t src_slot) {
+    return c_guard(HELP_E_NOMEM, [&] { return help_pcg_share_solution_body(dst, dst_slot, src, src_slot); });
 }
 
 static int help_pcg_features_body(help_pcg* ctx, int32_t slot, float* x) {

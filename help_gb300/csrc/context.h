@@ -142,6 +142,10 @@ struct help_pcg {
     bool x2_have[2][help::kSolveSlots] = {};
     int x2_cur = 0;
     int solve_slot = 0;
+    // slot of the i-th solve after a renew (help_pcg_set_solve_slots); past
+    // slot_map_n, solve i takes slot min(i, kSolveSlots - 1)
+    int32_t slot_map[help::kSolveSlots] = {};
+    int32_t slot_map_n = 0;
     help_pcg_stats stats{};
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     // CG graphs (one per precision), re-captured when their arguments change

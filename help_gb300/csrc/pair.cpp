@@ -9,7 +9,12 @@
 // Each context has its own stream and buffers, so the two CG runs overlap on
 // the GPU -- on small systems two single-cluster kernels on different SMs.
 // Construct and renew run on both contexts with the same arguments (renew on
-// two threads as well), so each solve gives what one context gives.
+// two threads as well), so each solve gives what one context gives.  With a
+// model attached (the learned part) the solve slots follow the systems as on
+// one context -- context 0's solves take slots 0 (bottom) and 2 (corrector),
+// context 1's slot 1 (predictor) -- and before each renew context 1 receives
+// context 0's bottom solution, whose features set the Schur-diagonal
+// correction: every warm start, feature and correction is one context's.
 #include <thread>
 
 #include "../../include/help_gpu.h"
@@ -44,8 +49,11 @@ int help_pcg_pair_create(const help_pcg_options* opt, help_pcg_pair** out) {
         // a warm start depends on the order of the solves, which the pair changes
         if (opt && opt->warm_start) return HELP_E_ARG;
         help_pcg_pair* p = new help_pcg_pair();
+        static const int32_t slots0[2] = {0, 2}, slots1[1] = {1};
         for (int i = 0; i < 2; ++i) {
-            const int rc = help_pcg_create(opt, &p->c[i]);
+            int rc = help_pcg_create(opt, &p->c[i]);
+            if (rc == HELP_OK) rc = i == 0 ? help_pcg_set_solve_slots(p->c[0], slots0, 2)
+                                           : help_pcg_set_solve_slots(p->c[1], slots1, 1);
             if (rc != HELP_OK) {
                 help_pcg_pair_free(p);
                 return rc;
@@ -78,7 +86,13 @@ int help_pcg_pair_construct(void* pair, int32_t m, int32_t n, const int32_t* col
 int help_pcg_pair_renew(void* pair, const double* d) {
     help_pcg_pair* p = as_pair(pair);
     if (!p) return HELP_E_ARG;
-    return c_guard(HELP_E_NOMEM, [&]() -> int { return both([&](int i) -> int { return help_pcg_renew(p->c[i], d); }); });
+    return c_guard(HELP_E_NOMEM, [&]() -> int {
+        // the bottom system's solution of the renew ending now, which the next
+        // renew's features read on context 1 as on context 0
+        const int rc = help_pcg_share_solution(p->c[1], 0, p->c[0], 0);
+        if (rc != HELP_OK) return rc;
+        return both([&](int i) -> int { return help_pcg_renew(p->c[i], d); });
+    });
 }
 
 int help_pcg_pair_solve(void* pair, const double* d, const double* b_1, const double* b_2, double* x_1,

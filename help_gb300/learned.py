@@ -420,14 +420,10 @@ def evaluate(lp, pivots: int, params: np.ndarray | None, cg_tol: float = 1e-10, 
     records (seconds, rel gap, primal / dual infeasibility, CG iterations so
     far) at every iteration.  ``paired``: the bottom system and the first
     direction of every iteration solved together on two contexts
-    (GpuPairNormalEquations), the model attached to both.  Each context's
-    solve slots keep one role -- context 0 the bottom system then the
-    corrector, context 1 the predictor -- so every warm start comes from the
-    previous renew's solution of the same system, as on one context; the
-    Schur-diagonal correction, which a context computes at renew from its
-    first slot's features, follows the predictor's history on context 1
-    (the bottom system's on one context), so the run is close to, not
-    bitwise, the single context's."""
+    (GpuPairNormalEquations), the model attached to both: the pair maps
+    each system to the solve slot it takes on one context and hands context
+    1 the bottom system's solution before each renew, so the run is the
+    single context's."""
     from . import hsd
 
     mlp = Mlp(device, params) if params is not None else None

@@ -194,7 +194,7 @@ GPU_SYMBOLS = [
     "help_mlp_forward", "help_mlp_loss_grad", "help_mlp_train_step", "help_pcg_attach_mlp", "help_pcg_features",
     "help_pcg_pair_create", "help_pcg_pair_free", "help_pcg_pair_context", "help_pcg_pair_construct",
     "help_pcg_pair_renew", "help_pcg_pair_solve", "help_pcg_pair_solve2", "help_pcg_pair_destruct",
-    "help_pcg_pair_matvec",
+    "help_pcg_pair_matvec", "help_pcg_set_solve_slots", "help_pcg_share_solution",
 ]
 LP_SYMBOLS = [
     "help_lp_generate", "help_lp_free", "help_lp_write_mps", "help_csc_to_csr", "help_lp_read_mps",
@@ -246,6 +246,8 @@ def gpu_lib() -> C.CDLL:
         lib.help_pcg_pair_free.restype = None
         lib.help_pcg_pair_context.argtypes = [vp, i32]
         lib.help_pcg_pair_context.restype = vp
+        lib.help_pcg_set_solve_slots.argtypes = [vp, vp, i32]
+        lib.help_pcg_share_solution.argtypes = [vp, i32, vp, i32]
         lib.help_mlp_create.argtypes = [i32, C.POINTER(C.c_void_p)]
         lib.help_mlp_free.argtypes = [vp]
         lib.help_mlp_last_error.argtypes = [vp]

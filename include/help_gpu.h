@@ -166,6 +166,20 @@ int help_pcg_matvec_dev(help_pcg* ctx, int32_t op, int32_t fp32, const void* x, 
  * the device and added to dest once. */
 int help_pcg_matvec_acc(help_pcg* ctx, int32_t transpose, int32_t sign, const double* v, double* dest);
 
+/* The learned part's solve slots (the i-th solve after a renew takes slot
+ * min(i, 3); each slot's solution seeds the same slot's warm start and
+ * features at the next renew): slots[i] is the slot of solve i for i < n
+ * (n <= 4, slots in [0, 4)), the default beyond.  The paired backend
+ * maps context 0's solves to slots {0, 2} and context 1's to {1}, the slots
+ * those systems take on one context. */
+int help_pcg_set_solve_slots(help_pcg* ctx, const int32_t* slots, int32_t n);
+/* dst's solution of dst_slot in the current renew := src's of src_slot (both
+ * constructed with the same matrix on the same device; nothing without an
+ * attached model).  The paired backend gives context 1 context 0's solution
+ * of the bottom system (slot 0) before each renew, whose features -- and so
+ * the Schur-diagonal correction -- it reads. */
+int help_pcg_share_solution(help_pcg* dst, int32_t dst_slot, help_pcg* src, int32_t src_slot);
+
 /* Two contexts on one GPU for the HSD driver's paired solves (help_lp.h,
  * help_ne_backend.solve2).  Each IPM iteration solves the bottom system
  * (LinearEquationBottom, HSDSolver.cpp:226-261) and the first search
@@ -174,7 +188,8 @@ int help_pcg_matvec_acc(help_pcg* ctx, int32_t transpose, int32_t sign, const do
  * on its own host thread and stream, so the two CG runs overlap on the GPU
  * (two single-cluster runs on small systems).  Both contexts are built and
  * renewed from the same arguments; each solve gives what help_pcg_solve on
- * one context gives (a cold start each: no warm start, no learned part).
+ * one context gives (the option warm_start is refused; an attached model is
+ * followed through help_pcg_set_solve_slots and help_pcg_share_solution).
  * The backend-table entries take the pair as their ctx. */
 typedef struct help_pcg_pair help_pcg_pair;
 int help_pcg_pair_create(const help_pcg_options* opt, help_pcg_pair** out);
