@@ -226,3 +226,23 @@ def test_hsd_driver_paired_solves_give_the_same_run():
     assert r1["solves"] == r2["solves"] and len(pairs) == r1["iterations"]
     assert r1["primal_obj"] == r2["primal_obj"] and r1["rel_gap"] == r2["rel_gap"]
     assert np.array_equal(r1["x"], r2["x"]) and np.array_equal(r1["y"], r2["y"])
+
+
+def test_pair_and_slot_entry_points_reject_bad_arguments():
+    """The paired backend and the solve-slot entry points check their
+    arguments before any device work (no GPU needed): a pair refuses the
+    warm_start option, null contexts and out-of-range slots are errors."""
+    import ctypes as C
+    from help_gb300 import backend, native
+    lib = native.gpu_lib()
+    opt = backend.pcg_options(lib, pivots=4, warm_start=True)
+    out = C.c_void_p()
+    assert lib.help_pcg_pair_create(C.byref(opt), C.byref(out)) == native.HELP_E_ARG and not out.value
+    slots = (C.c_int32 * 2)(0, 7)
+    assert lib.help_pcg_set_solve_slots(None, slots, 2) == native.HELP_E_ARG
+    assert lib.help_pcg_share_solution(None, 0, None, 0) == native.HELP_E_ARG
+    assert lib.help_pcg_pair_context(None, 0) is None
+    for fn in (lib.help_pcg_pair_renew, lib.help_pcg_pair_destruct):
+        fn.restype = C.c_int
+    assert lib.help_pcg_pair_renew(None, None) == native.HELP_E_ARG
+    assert lib.help_pcg_pair_destruct(None) == native.HELP_E_ARG
