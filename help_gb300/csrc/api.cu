@@ -1082,7 +1082,7 @@ static int help_pcg_solve_body(help_pcg* ctx, const double* d, const double* b_1
     if (!rc) rc = sumsq_host(ctx, ctx->rhs.as<double>(), m, &rhs2);
     if (rc) return rc;
     if (learned) {
-        // the plain preconditioner judges the model: redo cold and uncorrected
+        // the plain preconditioner is the model's fallback: redo cold and uncorrected
         // on an iteration cap or a failed FP64 residual check
         const double rel = rhs2 > 0.0 ? std::sqrt(rr / rhs2) : std::sqrt(rr);
         if (!converged || !(rel <= std::max(1e-6, 100.0 * ctx->opt.cg_tol))) {
