@@ -246,3 +246,24 @@ def test_pair_and_slot_entry_points_reject_bad_arguments():
         fn.restype = C.c_int
     assert lib.help_pcg_pair_renew(None, None) == native.HELP_E_ARG
     assert lib.help_pcg_pair_destruct(None) == native.HELP_E_ARG
+
+
+def test_hsd_driver_stops_on_a_failed_paired_solve():
+    """A backend whose solve2 fails ends the driver's run with the backend
+    error code (the same handling as a failed solve), after one call."""
+    import ctypes as C
+    from help_gb300 import native
+    lp = L.generate(L.spec_random(60, 180, 5), 4)
+    ora = ob.OracleNormalEquations(pivots=10, tol=1e-14, max_iter=10**6)
+    base = ora.ne_backend()
+    calls = []
+
+    def solve2(*_args):
+        calls.append(1)
+        return -1
+
+    fn = native.SOLVE2_FN(solve2)
+    be = native.NeBackend(ctx=base.ctx, construct=base.construct, renew=base.renew, solve=base.solve,
+                          destruct=base.destruct, solve2=C.cast(fn, C.c_void_p).value)
+    r = hsd.solve_lp(lp, be)
+    assert r["rc"] == -2 and len(calls) == 1
